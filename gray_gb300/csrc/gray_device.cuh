@@ -1,0 +1,219 @@
+// gray_device.cuh -- device-side arithmetic shared by the gray_gb300 kernels.
+//
+// Every expression here is evaluated exactly as written: the library is compiled with
+// -fmad=false (no implicit FMA contraction) and without --use_fast_math, and fmaf appears
+// only where an FMA is intended.  Together with the project's own exp/log below this makes
+// hit lists, fp16 keys and composited transmittance reproducible bit-for-bit on the CPU.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "../../include/gray_gb300.h"
+
+#define GRAY_LEAF_BIT 0x80000000u
+#define GRAY_NULL 0xFFFFFFFFu
+
+namespace gray {
+
+// ---------------------------------------------------------------------------------------------
+// exp: Cody & Waite argument reduction (x = k ln2 + r, |r| <= ln2/2, ln2 carried as two floats)
+// and the degree-7 Taylor polynomial of e^r in Horner form; 2^k applied through the exponent
+// field (two steps for results in the subnormal range).
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ float gexp(float x) {
+    if (x != x) return x;
+    if (x > 89.0f) return __int_as_float(0x7f800000);
+    if (x < -104.0f) return 0.0f;
+    float k = rintf(x * 0x1.715476p+0f);
+    float r = fmaf(-k, 0x1.62ep-1f, x);
+    r = fmaf(-k, 0x1.0bfbe8p-15f, r);
+    float p = 0x1.a01a02p-13f;
+    p = fmaf(p, r, 0x1.6c16c2p-10f);
+    p = fmaf(p, r, 0x1.111112p-7f);
+    p = fmaf(p, r, 0x1.555556p-5f);
+    p = fmaf(p, r, 0x1.555556p-3f);
+    p = fmaf(p, r, 0x1.0p-1f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    int ki = (int)k;
+    if (ki > 127) {
+        p = p * 2.0f;
+        ki -= 1;
+    }
+    if (ki < -126) {
+        p = p * __int_as_float((ki + 64 + 127) << 23);
+        return p * 0x1.0p-64f;
+    }
+    return p * __int_as_float((ki + 127) << 23);
+}
+
+// log: x = m 2^e, m in [sqrt(1/2), sqrt(2)]; log m = 2 atanh(s), s = (m-1)/(m+1), series to s^11.
+__device__ __forceinline__ float glog(float x) {
+    if (x != x) return x;
+    if (x < 0.0f) return __int_as_float(0x7fc00000);
+    if (x == 0.0f) return __int_as_float(0xff800000);
+    if (x == __int_as_float(0x7f800000)) return x;
+    uint32_t u = __float_as_uint(x);
+    int e = 0;
+    if (u < 0x00800000u) {
+        x = x * 0x1.0p23f;
+        u = __float_as_uint(x);
+        e = -23;
+    }
+    e += (int)(u >> 23) - 127;
+    float m = __uint_as_float((u & 0x007fffffu) | 0x3f800000u);
+    if (m > 0x1.6a09e6p+0f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    float f = m - 1.0f;
+    float s = f / (2.0f + f);
+    float z = s * s;
+    float q = 0x1.745d18p-4f;
+    q = fmaf(q, z, 0x1.c71c72p-4f);
+    q = fmaf(q, z, 0x1.24924ap-3f);
+    q = fmaf(q, z, 0x1.99999ap-3f);
+    q = fmaf(q, z, 0x1.555556p-2f);
+    float two_s = 2.0f * s;
+    float lm = fmaf(two_s * z, q, two_s);
+    float ef = (float)e;
+    return fmaf(ef, 0x1.62ep-1f, fmaf(ef, 0x1.0bfbe8p-15f, lm));
+}
+
+__device__ __forceinline__ float gpow(float a, float b) { return gexp(b * glog(a)); }
+
+__device__ __forceinline__ float sigmoid_act(float x) { return 1.0f / (1.0f + gexp(-x)); }
+
+// MAX_ALPHA (the double 0.9999) * a * b with a single final rounding: a*b split exactly by an
+// FMA, 0.9999 carried as a float pair.
+__device__ __forceinline__ float maxalpha_mul(float a, float b) {
+    const float c_hi = 0x1.fff2e4p-1f, c_lo = 0x1.1d14e4p-26f;
+    float p = a * b;
+    float e = fmaf(a, b, -p);
+    return fmaf(c_hi, p, fmaf(c_hi, e, c_lo * p));
+}
+
+// Scaling factor that clips the Gaussian where its alpha falls to alpha_threshold
+// (reference: cuda/utils/kernel.cu:3-22).
+__device__ __forceinline__ float scaling_factor(float opacity, float alpha_threshold, float exp_power) {
+    if (opacity <= alpha_threshold) return 0.0f;
+    float log_ratio = glog(opacity / alpha_threshold);
+    if (exp_power == 1.0f) return sqrtf(2.0f * log_ratio);
+    if (exp_power == 2.0f) return sqrtf(sqrtf(4.0f * log_ratio));
+    if (exp_power == 3.0f) {
+        float v = sqrtf(6.0f * log_ratio);
+        return v == 0.0f ? 0.0f : gexp(glog(v) * 0x1.555556p-2f);
+    }
+    float k = 2.0f * exp_power;
+    return gpow(k * log_ratio, 1.0f / k);
+}
+
+// Gaussian response at squared local radius d (reference: cuda/utils/kernel.cu:24-38).
+__device__ __forceinline__ float eval_gaussian(float d, float exp_power) {
+    if (exp_power == 1.0f) return gexp(-0.5f * d);
+    if (exp_power == 2.0f) return gexp(-0.25f * d * d);
+    if (exp_power == 3.0f) return gexp(-(d * d * d) / 6.0f);
+    float k = 2.0f * exp_power;
+    return gexp(-gpow(d, exp_power) / k);
+}
+
+// beta^n rounded to float (binary exponentiation in double), for Adam's bias correction.
+__device__ __forceinline__ float adam_pow(float beta, int n) {
+    double b = (double)beta, r = 1.0;
+    unsigned int k = (unsigned int)(n < 0 ? 0 : n);
+    while (k) {
+        if (k & 1u) r *= b;
+        b *= b;
+        k >>= 1;
+    }
+    return (float)r;
+}
+
+// Fixed-point form of one all-hit sum term: v * scale truncated toward zero (clamped, NaN -> 0).
+__device__ __forceinline__ long long to_fixed(float v, float scale) {
+    float t = v * scale;
+    if (!(t == t)) t = 0.0f;
+    t = fminf(fmaxf(t, -0x1.0p62f), 0x1.0p62f);
+    return __float2ll_rz(t);
+}
+
+__device__ __forceinline__ uint16_t f2h_bits(float f) { return __half_as_ushort(__float2half_rn(f)); }
+__device__ __forceinline__ float h2f_bits(uint16_t h) { return __half2float(__ushort_as_half(h)); }
+
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// Object-space ray of one Gaussian and the max-density point (reference:
+// cuda/shaders.cu:17-49).  g0..g2 = rows (M | mu) of the snapshot.
+struct LocalHit {
+    f3 lo, ld;      // object-space origin and (unnormalised) direction
+    float nrm;      // |ld|
+    f3 dn;          // ld / nrm
+    float s;        // distance along dn to the max-density point
+    f3 u;           // max-density point (unit-sphere frame)
+};
+
+__device__ __forceinline__ void local_ray(const float4 g0, const float4 g1, const float4 g2, f3 ro, f3 rd,
+                                          LocalHit &h) {
+    f3 rel = mk3(ro.x - g0.w, ro.y - g1.w, ro.z - g2.w);
+    h.lo = mk3(g0.x * rel.x + g0.y * rel.y + g0.z * rel.z, g1.x * rel.x + g1.y * rel.y + g1.z * rel.z,
+               g2.x * rel.x + g2.y * rel.y + g2.z * rel.z);
+    h.ld = mk3(g0.x * rd.x + g0.y * rd.y + g0.z * rd.z, g1.x * rd.x + g1.y * rd.y + g1.z * rd.z,
+               g2.x * rd.x + g2.y * rd.y + g2.z * rd.z);
+}
+
+__device__ __forceinline__ void closest_point(LocalHit &h) {
+    h.nrm = sqrtf(dot3(h.ld, h.ld));
+    h.dn = mk3(h.ld.x / h.nrm, h.ld.y / h.nrm, h.ld.z / h.nrm);
+    h.s = -h.lo.x * h.dn.x + -h.lo.y * h.dn.y + -h.lo.z * h.dn.z;
+    h.u = mk3(h.lo.x + h.s * h.dn.x, h.lo.y + h.s * h.dn.y, h.lo.z + h.s * h.dn.z);
+}
+
+// Segment [znear, zfar] of the object-space ray against the instance's unit box [-1, 1]^3 (the
+// candidate test OptiX applies before the intersection program).
+__device__ __forceinline__ bool unit_box_overlap(const LocalHit &h, float znear, float zfar) {
+    float t0 = znear, t1 = zfar;
+    const float lo[3] = {h.lo.x, h.lo.y, h.lo.z}, ld[3] = {h.ld.x, h.ld.y, h.ld.z};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float inv = 1.0f / ld[k];
+        float ta = (-1.0f - lo[k]) * inv, tb = (1.0f - lo[k]) * inv;
+        t0 = fmaxf(t0, fminf(ta, tb));
+        t1 = fminf(t1, fmaxf(ta, tb));
+    }
+    return t0 <= t1;
+}
+
+// Intersection program (reference: cuda/shaders.cu:10-67) for one (ray, Gaussian) pair.
+// o = live opacity (or -inf if the snapshot marked the Gaussian invisible), sf = live scaling
+// factor.  Returns true on a hit with the world distance and fp32 alpha.
+__device__ __forceinline__ bool intersect(const float4 g0, const float4 g1, const float4 g2, float o, float sf, f3 ro,
+                                          f3 rd, float alpha_threshold, float exp_power, float znear, float zfar,
+                                          float &dist, float &alpha) {
+    if (o <= alpha_threshold) return false;
+    LocalHit h;
+    local_ray(g0, g1, g2, ro, rd, h);
+    if (dot3(h.lo, h.ld) > 0.0f) return false;
+    closest_point(h);
+    float sq = dot3(h.u, h.u);
+    if (sq > 1.0f) return false;
+    dist = h.s / h.nrm;
+    if (!(dist >= znear && dist <= zfar)) {
+        if (!unit_box_overlap(h, znear, zfar)) return false;
+    }
+    f3 x = mk3(h.u.x * sf, h.u.y * sf, h.u.z * sf);
+    float gv = eval_gaussian(dot3(x, x), exp_power);
+    alpha = maxalpha_mul(gv, o);
+    return true;
+}
+
+// Device-side error reporting: bits are OR-ed into a status word; the host reads it later.
+__device__ __forceinline__ void raise_status(int32_t *status, int32_t bits) {
+    if (status) atomicOr(status, bits);
+}
+
+}  // namespace gray

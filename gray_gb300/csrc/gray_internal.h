@@ -1,0 +1,34 @@
+// gray_internal.h -- launchers shared between the translation units of libgray_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gray_gb300.h"
+
+namespace gray {
+
+// scene.cu
+cudaError_t launch_snapshot(const gray_params &p, cudaStream_t s);
+// reset_frame: zero was_visible, count the call and empty the backward hit list (forward_pass)
+cudaError_t launch_forward_prep(const gray_params &p, bool reset_frame, cudaStream_t s);
+cudaError_t launch_fold_and_sh_backward(const gray_params &p, cudaStream_t s);
+
+// lbvh.cu
+cudaError_t launch_lbvh_build(const gray_params &p, cudaStream_t s);
+cudaError_t launch_lbvh_refit(const gray_params &p, cudaStream_t s);
+size_t sort_tmp_words(int n);
+
+// trace.cu
+cudaError_t launch_trace_forward(const gray_params &p, cudaStream_t s);
+cudaError_t launch_trace_backward(const gray_params &p, cudaStream_t s);
+
+// adam.cu
+cudaError_t launch_adam(const gray_params &p, cudaStream_t s);
+
+constexpr int kThreads = 256;
+inline unsigned int blocks_for(long long n, int threads = kThreads) {
+    return (unsigned int)((n + threads - 1) / threads);
+}
+
+}  // namespace gray

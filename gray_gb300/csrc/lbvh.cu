@@ -1,0 +1,356 @@
+// lbvh.cu -- linear BVH over the Gaussians' leaf boxes (replaces the OptiX instance
+// acceleration structure built in cuda/optix/bvh_wrapper.h:89-115 and refit in :25-39).
+//
+// Build: scene bounds of the leaf-box centroids -> 30-bit Morton codes -> stable LSD radix
+// sort of (code, gaussian id) with 8-bit digits (4 passes, no CUB) -> Karras (2012)
+// hierarchy, one thread per internal node -> bottom-up boxes.
+// Refit: bottom-up boxes only; each internal node is finished by the second of its two
+// children to arrive (one atomic counter per node, no spinning).
+//
+// Node layout (16 floats): child0 box (minx miny minz maxx maxy maxz), child1 box, child0 link,
+// child1 link, pad, pad.  A link with GRAY_LEAF_BIT set names a Gaussian; otherwise an
+// internal node.  Everything here is deterministic; the CPU oracle restates it bit-exactly.
+#include "gray_device.cuh"
+#include "gray_internal.h"
+
+namespace gray {
+
+__device__ __forceinline__ uint32_t f2ord(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__global__ void bounds_init_kernel(uint32_t *bounds) {
+    int t = threadIdx.x;
+    if (t < 3) bounds[t] = 0xFFFFFFFFu;
+    else if (t < 6) bounds[t] = 0u;
+}
+
+__global__ void bounds_kernel(int n, const float4 *__restrict__ aabb, uint32_t *__restrict__ bounds) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float lo[3] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000)};
+    float hi[3] = {__int_as_float(0xff800000), __int_as_float(0xff800000), __int_as_float(0xff800000)};
+    if (i < n) {
+        float4 a = aabb[2 * i], b = aabb[2 * i + 1];
+        float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+        if (isfinite(c[0]) && isfinite(c[1]) && isfinite(c[2])) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                lo[k] = c[k];
+                hi[k] = c[k];
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], off));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], off));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            if (lo[k] <= hi[k]) {
+                atomicMin(&bounds[k], f2ord(lo[k]));
+                atomicMax(&bounds[3 + k], f2ord(hi[k]));
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t expand10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__global__ void morton_kernel(int n, const float4 *__restrict__ aabb, const uint32_t *__restrict__ bounds,
+                              uint32_t *__restrict__ codes, uint32_t *__restrict__ ids) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 a = aabb[2 * i], b = aabb[2 * i + 1];
+    float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+    bool fin = true;
+    uint32_t q[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        fin = fin && isfinite(c[k]);
+        float lo = ord2f(bounds[k]), hi = ord2f(bounds[3 + k]);
+        float ext = hi - lo;
+        float t = ext > 0.0f ? (c[k] - lo) / ext : 0.0f;
+        float s = fminf(fmaxf(t * 1024.0f, 0.0f), 1023.0f);
+        q[k] = fin ? (uint32_t)s : 0u;
+    }
+    codes[i] = fin ? ((expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2])) : 0x40000000u;
+    ids[i] = (uint32_t)i;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Stable LSD radix sort, 8-bit digits.  A tile is kSortThreads x kSortItems keys processed in
+// kSortItems rounds of kSortThreads consecutive keys, so tile order == round-major order.
+// ---------------------------------------------------------------------------------------------
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kSortWarps = kSortThreads / 32;
+
+size_t sort_tmp_words(int n) {
+    size_t tiles = (size_t)((n + kSortTile - 1) / kSortTile);
+    return 2 * (size_t)n + 256 * (tiles > 0 ? tiles : 1);
+}
+
+__global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(int n, int shift, const uint32_t *__restrict__ keys,
+                                                                 uint32_t *__restrict__ counts, int tiles) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile;
+#pragma unroll
+    for (int r = 0; r < kSortItems; r++) {
+        int idx = base + r * kSortThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    counts[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// exclusive scan of counts[256 * tiles] (digit-major) by one block
+__global__ void __launch_bounds__(1024) radix_scan_kernel(uint32_t *__restrict__ counts, int total) {
+    __shared__ uint32_t part[1024];
+    const int t = threadIdx.x;
+    const int chunk = (total + 1023) / 1024;
+    const int b = t * chunk, e = min(b + chunk, total);
+    uint32_t s = 0;
+    for (int i = b; i < e; i++) s += counts[i];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        uint32_t v = t >= off ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[t] - s;
+    for (int i = b; i < e; i++) {
+        uint32_t c = counts[i];
+        counts[i] = run;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(int n, int shift,
+                                                                    const uint32_t *__restrict__ keys_in,
+                                                                    const uint32_t *__restrict__ vals_in,
+                                                                    uint32_t *__restrict__ keys_out,
+                                                                    uint32_t *__restrict__ vals_out,
+                                                                    const uint32_t *__restrict__ offsets, int tiles) {
+    __shared__ uint32_t warp_cnt[kSortWarps][256];
+    __shared__ uint32_t digit_run[256];
+    __shared__ uint32_t digit_off[256];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    digit_run[t] = 0;
+    digit_off[t] = offsets[t * tiles + blockIdx.x];
+    const uint32_t lanemask_lt = (1u << lane) - 1u;
+    const int base = blockIdx.x * kSortTile;
+    for (int r = 0; r < kSortItems; r++) {
+#pragma unroll
+        for (int w = 0; w < kSortWarps; w++) warp_cnt[w][t] = 0;
+        __syncthreads();
+        const int idx = base + r * kSortThreads + t;
+        const bool valid = idx < n;
+        uint32_t key = valid ? keys_in[idx] : 0u, val = valid ? vals_in[idx] : 0u;
+        uint32_t digit = valid ? (key >> shift) & 0xFFu : 256u + (uint32_t)lane;  // invalid lanes never match
+        uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        uint32_t rank = __popc(peers & lanemask_lt);
+        if (valid && rank == 0) warp_cnt[warp][digit] = __popc(peers);
+        __syncthreads();
+        {   // per digit: exclusive prefix over warps, continuing the tile's running count
+            uint32_t run = digit_run[t];
+#pragma unroll
+            for (int w = 0; w < kSortWarps; w++) {
+                uint32_t c = warp_cnt[w][t];
+                warp_cnt[w][t] = run;
+                run += c;
+            }
+            digit_run[t] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = digit_off[digit] + warp_cnt[warp][digit] + rank;
+            keys_out[pos] = key;
+            vals_out[pos] = val;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Karras (2012) hierarchy over sorted codes; ties broken by sorted position.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ int lbvh_delta(const uint32_t *codes, int n, int i, int j) {
+    if (j < 0 || j > n - 1) return -1;
+    uint32_t a = codes[i], b = codes[j];
+    if (a == b) return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+    return __clz(a ^ b);
+}
+
+__global__ void karras_kernel(int n, const uint32_t *__restrict__ codes, const uint32_t *__restrict__ order,
+                              float *__restrict__ nodes, int32_t *__restrict__ int_parent,
+                              int32_t *__restrict__ leaf_parent) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = lbvh_delta(codes, n, i, i + 1) - lbvh_delta(codes, n, i, i - 1) >= 0 ? 1 : -1;
+    int dmin = lbvh_delta(codes, n, i, i - d);
+    int lmax = 2;
+    while (lbvh_delta(codes, n, i, i + lmax * d) > dmin) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (lbvh_delta(codes, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = lbvh_delta(codes, n, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) / 2;
+        if (lbvh_delta(codes, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int gamma = i + s * d + (d < 0 ? d : 0);
+    int lo_i = min(i, j), hi_i = max(i, j);
+    uint32_t c0, c1;
+    if (lo_i == gamma) {
+        c0 = order[gamma] | GRAY_LEAF_BIT;
+        leaf_parent[gamma] = i;
+    } else {
+        c0 = (uint32_t)gamma;
+        int_parent[gamma] = i;
+    }
+    if (hi_i == gamma + 1) {
+        c1 = order[gamma + 1] | GRAY_LEAF_BIT;
+        leaf_parent[gamma + 1] = i;
+    } else {
+        c1 = (uint32_t)(gamma + 1);
+        int_parent[gamma + 1] = i;
+    }
+    float4 *nd = reinterpret_cast<float4 *>(nodes) + 4 * (size_t)i;
+    nd[3] = make_float4(__uint_as_float(c0), __uint_as_float(c1), 0.0f, 0.0f);
+    if (i == 0) int_parent[0] = -1;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Bottom-up boxes.  One thread per sorted leaf; the second child to reach a node unions the
+// two child boxes and carries on to the parent.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void store_child_box(float *nodes, int node, int slot, const float b[6]) {
+    float *nd = nodes + 16 * (size_t)node + 6 * slot;
+#pragma unroll
+    for (int k = 0; k < 6; k++) __stcg(nd + k, b[k]);
+}
+
+__global__ void refit_kernel(int n, const float4 *__restrict__ aabb, const uint32_t *__restrict__ order,
+                             const int32_t *__restrict__ leaf_parent, const int32_t *__restrict__ int_parent,
+                             float *__restrict__ nodes, uint32_t *__restrict__ flags, float *__restrict__ root_box) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t gid = order[k];
+    float4 a = aabb[2 * gid], b = aabb[2 * gid + 1];
+    float box[6] = {a.x, a.y, a.z, b.x, b.y, b.z};
+    int p = n > 1 ? leaf_parent[k] : -1;
+    if (p < 0) {
+        root_box[0] = box[0];
+        root_box[1] = box[1];
+        root_box[2] = box[2];
+        root_box[3] = 0.0f;
+        root_box[4] = box[3];
+        root_box[5] = box[4];
+        root_box[6] = box[5];
+        root_box[7] = 0.0f;
+        return;
+    }
+    uint32_t link = gid | GRAY_LEAF_BIT;
+    for (int guard = 0; guard < 128; guard++) {
+        uint32_t c0 = __float_as_uint(__ldcg(nodes + 16 * (size_t)p + 12));
+        store_child_box(nodes, p, c0 == link ? 0 : 1, box);
+        __threadfence();
+        if (atomicAdd(&flags[p], 1u) == 0u) return;
+        __threadfence();
+        const float *nd = nodes + 16 * (size_t)p;
+        float u[6];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            u[q] = fminf(__ldcg(nd + q), __ldcg(nd + 6 + q));
+            u[3 + q] = fmaxf(__ldcg(nd + 3 + q), __ldcg(nd + 9 + q));
+        }
+#pragma unroll
+        for (int q = 0; q < 6; q++) box[q] = u[q];
+        int pp = int_parent[p];
+        if (pp < 0) {
+            root_box[0] = box[0];
+            root_box[1] = box[1];
+            root_box[2] = box[2];
+            root_box[3] = 0.0f;
+            root_box[4] = box[3];
+            root_box[5] = box[4];
+            root_box[6] = box[5];
+            root_box[7] = 0.0f;
+            return;
+        }
+        link = (uint32_t)p;
+        p = pp;
+    }
+}
+
+cudaError_t launch_lbvh_refit(const gray_params &p, cudaStream_t s) {
+    const int n = p.gaussians.count;
+    if (n <= 0) return cudaSuccess;
+    const gray_scene &sc = p.scene;
+    if (n > 1) {
+        cudaError_t e = cudaMemsetAsync(sc.refit_flags, 0, sizeof(uint32_t) * (size_t)(n - 1), s);
+        if (e != cudaSuccess) return e;
+    }
+    refit_kernel<<<blocks_for(n), kThreads, 0, s>>>(n, reinterpret_cast<const float4 *>(sc.aabb), sc.order,
+                                                   sc.leaf_parent, sc.int_parent, sc.nodes, sc.refit_flags,
+                                                   sc.root_box);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lbvh_build(const gray_params &p, cudaStream_t s) {
+    const int n = p.gaussians.count;
+    if (n <= 0) return cudaSuccess;
+    const gray_scene &sc = p.scene;
+    cudaError_t e;
+    bounds_init_kernel<<<1, 32, 0, s>>>(sc.bounds);
+    bounds_kernel<<<blocks_for(n), kThreads, 0, s>>>(n, reinterpret_cast<const float4 *>(sc.aabb), sc.bounds);
+    morton_kernel<<<blocks_for(n), kThreads, 0, s>>>(n, reinterpret_cast<const float4 *>(sc.aabb), sc.bounds, sc.codes,
+                                                    sc.order);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const int tiles = (n + kSortTile - 1) / kSortTile;
+    uint32_t *keys_alt = sc.sort_tmp, *vals_alt = sc.sort_tmp + n, *counts = sc.sort_tmp + 2 * (size_t)n;
+    uint32_t *kin = sc.codes, *vin = sc.order, *kout = keys_alt, *vout = vals_alt;
+    for (int shift = 0; shift < 32; shift += 8) {
+        radix_hist_kernel<<<tiles, kSortThreads, 0, s>>>(n, shift, kin, counts, tiles);
+        radix_scan_kernel<<<1, 1024, 0, s>>>(counts, 256 * tiles);
+        radix_scatter_kernel<<<tiles, kSortThreads, 0, s>>>(n, shift, kin, vin, kout, vout, counts, tiles);
+        uint32_t *tk = kin, *tv = vin;
+        kin = kout;
+        vin = vout;
+        kout = tk;
+        vout = tv;
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // four passes: the sorted keys/ids are back in codes/order
+    if (n > 1) {
+        karras_kernel<<<blocks_for(n - 1), kThreads, 0, s>>>(n, sc.codes, sc.order, sc.nodes, sc.int_parent,
+                                                            sc.leaf_parent);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return launch_lbvh_refit(p, s);
+}
+
+}  // namespace gray

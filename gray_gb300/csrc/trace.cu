@@ -1,0 +1,647 @@
+// trace.cu -- forward and backward ray tracing of the Gaussians on the LBVH.
+//
+// Forward (replaces the OptiX launch of cuda/shaders.cu:69-106 with cuda/forward_pass.cu):
+//   A warp traces an 8x4 pixel tile as one packet: the traversal stack is warp-uniform (held
+//   across the lanes' registers), every lane tests its own ray against both child boxes of the
+//   popped node and the warp descends where any lane hits.  Leaves run the intersection
+//   program of cuda/shaders.cu:10-67 per lane.  The first traversal accumulates, over ALL hits,
+//   the full transmittance and (in 64-bit fixed point) the alpha-weighted colour sums the
+//   reference uses for its truncated-tail estimate, and every traversal keeps the KB nearest
+//   hits above a resume key in a per-lane shared-memory buffer of 64-bit keys
+//   (fp16 distance | gaussian id | fp16 alpha).  The buffer is consumed by a state machine that
+//   reproduces the reference's 32-slot multi-pass selection exactly (pass boundaries, the
+//   strict `distance > tmin` drop of equal distances, the 99-pass cap, zfar, t_threshold).
+//   Composited ids are appended to the backward hit list in warp-aggregated segments.
+// Backward (cuda/backward_pass.cu:2-142): one thread per pixel walks its segments back to front,
+//   recomputes alpha in fp32 and reduces the 16 per-hit gradient values into the per-Gaussian
+//   accumulator with four 16-byte vector reductions.
+#include "gray_device.cuh"
+#include "gray_internal.h"
+
+namespace gray {
+
+constexpr int kTileW = 8, kTileH = 4;        // one warp
+constexpr int kBlockWarpsX = 2, kBlockWarpsY = 2;
+constexpr int kWarps = kBlockWarpsX * kBlockWarpsY;
+constexpr int kBlockW = kTileW * kBlockWarpsX, kBlockH = kTileH * kBlockWarpsY;
+constexpr int kFwdThreads = kWarps * 32;
+constexpr int kStackWords = 2;               // warp-uniform stack of 64 entries in 2 registers per lane
+constexpr int kStackMax = 32 * kStackWords;
+constexpr int kPassSlots = 32;               // BUFFER_SIZE, cuda/forward_pass.cu:4
+constexpr int kMaxPasses = 99;               // MAX_ITERATIONS, cuda/forward_pass.cu:3
+constexpr int kMaxTraversals = 4 * kMaxPasses;  // bound on re-traversals of one ray
+constexpr unsigned kFull = 0xffffffffu;
+
+struct FwdArgs {
+    uint32_t alloc_w, render_w, render_h;
+    int n;
+    const float *cam_origin, *fov, *w2c, *znear, *zfar;
+    const float *exp_power, *alpha_threshold, *t_threshold, *eps_fwd, *bg;
+    const uint8_t *render_depth, *needs_ray_output, *rays_from_python, *jitter, *grads_enabled;
+    const uint32_t *total_num_calls;
+    const float4 *geom;
+    const float2 *live;
+    const float *channels;
+    const float4 *nodes;
+    const float *root_box;
+    float *out_rgb, *out_depth, *out_T, *out_fullT, *out_rem, *ray_o, *ray_d;
+    int32_t *stat_hit, *stat_acc;
+    uint32_t *head, *counter, *pool;
+    uint32_t pool_size;
+    int32_t *status;
+};
+
+// PCG32 output hash (O'Neill 2014) for the optional sub-pixel jitter.
+__device__ __forceinline__ uint32_t pcg_hash(uint32_t v) {
+    uint32_t state = v * 747796405u + 2891336453u;
+    uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+
+__device__ __forceinline__ bool slab_hit(const float bmin[3], const float bmax[3], f3 ro, f3 inv, float eps) {
+    float ta = (bmin[0] - eps - ro.x) * inv.x, tb = (bmax[0] + eps - ro.x) * inv.x;
+    float tn = fminf(ta, tb), tf = fmaxf(ta, tb);
+    ta = (bmin[1] - eps - ro.y) * inv.y;
+    tb = (bmax[1] + eps - ro.y) * inv.y;
+    tn = fmaxf(tn, fminf(ta, tb));
+    tf = fminf(tf, fmaxf(ta, tb));
+    ta = (bmin[2] - eps - ro.z) * inv.z;
+    tb = (bmax[2] + eps - ro.z) * inv.z;
+    tn = fmaxf(tn, fminf(ta, tb));
+    tf = fminf(tf, fmaxf(ta, tb));
+    return tn <= tf && tf >= 0.0f;
+}
+
+struct LaneState {
+    // all-hit accumulators (first traversal only)
+    float ft;
+    long long afx, cfx0, cfx1, cfx2;
+    int nhit;
+    // selection buffer of the current traversal
+    int kcount, ncand;
+    unsigned long long kmax;
+    // resume key for the next traversal
+    unsigned long long resume;
+    bool has_resume;
+};
+
+template <int KB>
+__device__ __forceinline__ void on_leaf(const FwdArgs &a, uint32_t gid, bool want, bool first, f3 ro, f3 rd,
+                                        float athr, float pw, float znear, float zfar, LaneState &st,
+                                        unsigned long long (*kbuf)[kFwdThreads]) {
+    if (!want) return;
+    const float4 g0 = a.geom[3 * gid], g1 = a.geom[3 * gid + 1], g2 = a.geom[3 * gid + 2];
+    const float2 lv = a.live[gid];
+    float dist, alpha;
+    if (!intersect(g0, g1, g2, lv.x, lv.y, ro, rd, athr, pw, znear, zfar, dist, alpha)) return;
+    const uint16_t a16 = f2h_bits(alpha), d16 = f2h_bits(dist);
+    if (first) {
+        st.ft = fmaf(-st.ft, alpha, st.ft);
+        const float af = h2f_bits(a16);
+        const float *c = a.channels + 3 * (size_t)gid;
+        st.afx += to_fixed(af, 0x1.0p24f);
+        st.cfx0 += to_fixed(af * c[0], 0x1.0p32f);
+        st.cfx1 += to_fixed(af * c[1], 0x1.0p32f);
+        st.cfx2 += to_fixed(af * c[2], 0x1.0p32f);
+        st.nhit++;
+    }
+    if (!(h2f_bits(d16) > znear)) return;
+    const unsigned long long key =
+        ((unsigned long long)d16 << 48) | ((unsigned long long)gid << 16) | (unsigned long long)a16;
+    if (st.has_resume && !(key > st.resume)) return;
+    st.ncand++;
+    const int t = threadIdx.x;
+    int pos;
+    if (st.kcount < KB) {
+        pos = st.kcount++;
+    } else if (key < st.kmax) {
+        pos = KB - 1;
+    } else {
+        return;
+    }
+    while (pos > 0) {
+        unsigned long long prev = kbuf[pos - 1][t];
+        if (prev < key) break;
+        kbuf[pos][t] = prev;
+        pos--;
+    }
+    kbuf[pos][t] = key;
+    if (st.kcount == KB) st.kmax = kbuf[KB - 1][t];
+}
+
+template <int KB>
+__global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArgs a) {
+    __shared__ unsigned long long kbuf[KB][kFwdThreads];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int px = blockIdx.x * kBlockW + (warp % kBlockWarpsX) * kTileW + (lane % kTileW);
+    const int py = blockIdx.y * kBlockH + (warp / kBlockWarpsX) * kTileH + (lane / kTileW);
+    const bool inside = px < (int)a.render_w && py < (int)a.render_h;
+    const uint32_t pixel = (uint32_t)py * a.alloc_w + (uint32_t)px;
+
+    const float znear = *a.znear, zfar = *a.zfar;
+    const float athr = *a.alpha_threshold, pw = *a.exp_power, tthr = *a.t_threshold;
+    const bool grads = *a.grads_enabled != 0;
+    const bool render_depth = *a.render_depth != 0;
+
+    // ---- ray generation (cuda/shaders.cu:76-88, cuda/core/camera.h:17-36) ----
+    f3 ro = mk3(0.0f, 0.0f, 0.0f), rd = mk3(0.0f, 0.0f, 0.0f);
+    bool alive = false;
+    if (inside) {
+        if (*a.rays_from_python) {
+            ro = mk3(a.ray_o[3 * pixel], a.ray_o[3 * pixel + 1], a.ray_o[3 * pixel + 2]);
+            rd = mk3(a.ray_d[3 * pixel], a.ray_d[3 * pixel + 1], a.ray_d[3 * pixel + 2]);
+        } else {
+            ro = mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]);
+            const float view_size = tanf(*a.fov / 2.0f);
+            const float aspect = (float)a.render_w / (float)a.render_h;
+            float fx = (float)px, fy = (float)py;
+            if (*a.jitter) {
+                uint32_t h = pcg_hash(pixel ^ pcg_hash(*a.total_num_calls));
+                fx = fx + ((float)(h & 0xFFFFu) * 0x1.0p-16f - 0.5f);
+                fy = fy + ((float)(h >> 16) * 0x1.0p-16f - 0.5f);
+            }
+            const float y = view_size * (1.0f - 2.0f * (fy + 0.5f) / (float)a.render_h);
+            const float x = aspect * view_size * (2.0f * (fx + 0.5f) / (float)a.render_w - 1.0f);
+            const float *w = a.w2c;
+            f3 v = mk3(w[0] * x + w[3] * y - w[6], w[1] * x + w[4] * y - w[7], w[2] * x + w[5] * y - w[8]);
+            const float inv = 1.0f / sqrtf(dot3(v, v));
+            rd = mk3(v.x * inv, v.y * inv, v.z * inv);
+        }
+        alive = !(sqrtf(dot3(rd, rd)) == 0.0f);
+    }
+
+    LaneState st;
+    st.ft = 1.0f;
+    st.afx = st.cfx0 = st.cfx1 = st.cfx2 = 0;
+    st.nhit = 0;
+    st.kcount = 0;
+    st.ncand = 0;
+    st.kmax = 0;
+    st.resume = 0;
+    st.has_resume = false;
+    float T = 1.0f, C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, depth = 0.0f;
+    int pass = 0, slots = 0, nacc = 0;
+    float tmin_sel = znear, last_d = znear;
+    bool done = !alive;
+    uint32_t head = GRAY_NULL;
+
+    f3 inv = mk3(0.0f, 0.0f, 0.0f);
+    {
+        float dx = fabsf(rd.x) < 1e-20f ? (rd.x < 0.0f ? -1e-20f : 1e-20f) : rd.x;
+        float dy = fabsf(rd.y) < 1e-20f ? (rd.y < 0.0f ? -1e-20f : 1e-20f) : rd.y;
+        float dz = fabsf(rd.z) < 1e-20f ? (rd.z < 0.0f ? -1e-20f : 1e-20f) : rd.z;
+        inv = mk3(1.0f / dx, 1.0f / dy, 1.0f / dz);
+    }
+    const float eps = 2.0e-6f * (fabsf(ro.x) + fabsf(ro.y) + fabsf(ro.z));
+    // packet lead direction for the near/far child order (any deterministic choice is valid)
+    float lx = alive ? rd.x : 0.0f, ly = alive ? rd.y : 0.0f, lz = alive ? rd.z : 0.0f;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        lx += __shfl_xor_sync(kFull, lx, off);
+        ly += __shfl_xor_sync(kFull, ly, off);
+        lz += __shfl_xor_sync(kFull, lz, off);
+    }
+
+    bool first = true;
+    int traversals = 0;
+    const int n = a.n;
+    while (__any_sync(kFull, !done)) {
+        const bool want = !done;
+        st.kcount = 0;
+        st.ncand = 0;
+        // ---------------- traversal ----------------
+        if (n == 1) {
+            const float *rb = a.root_box;
+            const float bmin[3] = {rb[0], rb[1], rb[2]}, bmax[3] = {rb[4], rb[5], rb[6]};
+            bool h = want && slab_hit(bmin, bmax, ro, inv, eps);
+            if (__any_sync(kFull, h)) on_leaf<KB>(a, 0u, h, first, ro, rd, athr, pw, znear, zfar, st, kbuf);
+        } else if (n > 1) {
+            uint32_t stk0 = 0, stk1 = 0;  // entry e lives in lane e%32, word e/32
+            int sp = 0;
+            {
+                const float *rb = a.root_box;
+                const float bmin[3] = {rb[0], rb[1], rb[2]}, bmax[3] = {rb[4], rb[5], rb[6]};
+                bool h = want && slab_hit(bmin, bmax, ro, inv, eps);
+                if (__any_sync(kFull, h)) {
+                    if (lane == 0) stk0 = 0u;
+                    sp = 1;
+                }
+            }
+            while (sp > 0) {
+                sp--;
+                const uint32_t word = (sp >> 5) == 0 ? stk0 : stk1;
+                const uint32_t node = __shfl_sync(kFull, word, sp & 31);
+                if (node >= (uint32_t)(n - 1)) {
+                    raise_status(a.status, GRAY_STATUS_STACK_OVERFLOW);
+                    continue;
+                }
+                const float4 q0 = a.nodes[4 * node], q1 = a.nodes[4 * node + 1], q2 = a.nodes[4 * node + 2],
+                             q3 = a.nodes[4 * node + 3];
+                const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
+                const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
+                const uint32_t c0 = __float_as_uint(q3.x), c1 = __float_as_uint(q3.y);
+                const bool h0 = want && slab_hit(b0min, b0max, ro, inv, eps);
+                const bool h1 = want && slab_hit(b1min, b1max, ro, inv, eps);
+                const bool any0 = __any_sync(kFull, h0), any1 = __any_sync(kFull, h1);
+                if (!any0 && !any1) continue;
+                // near child first along the packet's lead direction
+                const float p0 = (b0min[0] + b0max[0]) * lx + (b0min[1] + b0max[1]) * ly + (b0min[2] + b0max[2]) * lz;
+                const float p1 = (b1min[0] + b1max[0]) * lx + (b1min[1] + b1max[1]) * ly + (b1min[2] + b1max[2]) * lz;
+                const bool swap = p1 < p0;
+                const uint32_t cn = swap ? c1 : c0, cf = swap ? c0 : c1;
+                const bool an = swap ? any1 : any0, af = swap ? any0 : any1;
+                const bool hn = swap ? h1 : h0, hf = swap ? h0 : h1;
+                // far internal child goes deeper in the stack, near internal child on top;
+                // leaves are processed right away, near first
+                if (af && !(cf & GRAY_LEAF_BIT)) {
+                    if (sp < kStackMax) {
+                        if (lane == (sp & 31)) {
+                            if ((sp >> 5) == 0) stk0 = cf;
+                            else stk1 = cf;
+                        }
+                        sp++;
+                    } else {
+                        raise_status(a.status, GRAY_STATUS_STACK_OVERFLOW);
+                    }
+                }
+                if (an && (cn & GRAY_LEAF_BIT)) {
+                    const uint32_t gid = cn & ~GRAY_LEAF_BIT;
+                    if (gid < (uint32_t)n) on_leaf<KB>(a, gid, hn, first, ro, rd, athr, pw, znear, zfar, st, kbuf);
+                }
+                if (af && (cf & GRAY_LEAF_BIT)) {
+                    const uint32_t gid = cf & ~GRAY_LEAF_BIT;
+                    if (gid < (uint32_t)n) on_leaf<KB>(a, gid, hf, first, ro, rd, athr, pw, znear, zfar, st, kbuf);
+                }
+                if (an && !(cn & GRAY_LEAF_BIT)) {
+                    if (sp < kStackMax) {
+                        if (lane == (sp & 31)) {
+                            if ((sp >> 5) == 0) stk0 = cn;
+                            else stk1 = cn;
+                        }
+                        sp++;
+                    } else {
+                        raise_status(a.status, GRAY_STATUS_STACK_OVERFLOW);
+                    }
+                }
+            }
+        }
+        // ---------------- consume (cuda/forward_pass.cu:46-125) ----------------
+        int nc = 0;
+        if (want) {
+            const int t = threadIdx.x;
+            const unsigned long long last_key = st.kcount > 0 ? kbuf[st.kcount - 1][t] : 0ull;
+            for (int i = 0; i < st.kcount; i++) {
+                const unsigned long long key = kbuf[i][t];
+                const float d = h2f_bits((uint16_t)(key >> 48));
+                if (!(d > tmin_sel)) continue;
+                if (slots == kPassSlots) {
+                    pass++;
+                    if (pass >= kMaxPasses) {
+                        done = true;
+                        break;
+                    }
+                    tmin_sel = last_d;
+                    if (!(tmin_sel < zfar)) {
+                        done = true;
+                        break;
+                    }
+                    slots = 0;
+                    if (!(d > tmin_sel)) continue;
+                }
+                slots++;
+                last_d = d;
+                if (!(d < zfar)) {
+                    done = true;
+                    break;
+                }
+                const uint32_t gid = (uint32_t)(key >> 16);
+                const float al = h2f_bits((uint16_t)(key & 0xFFFFu));
+                const float *c = a.channels + 3 * (size_t)gid;
+                const float cx = c[0], cy = c[1], cz = c[2];
+                st.afx -= to_fixed(al, 0x1.0p24f);
+                st.cfx0 -= to_fixed(al * cx, 0x1.0p32f);
+                st.cfx1 -= to_fixed(al * cy, 0x1.0p32f);
+                st.cfx2 -= to_fixed(al * cz, 0x1.0p32f);
+                const float w = T * al;
+                C0 = C0 + cx * w;
+                C1 = C1 + cy * w;
+                C2 = C2 + cz * w;
+                if (render_depth) depth = depth + d * w;
+                T = T * (1.0f - al);
+                kbuf[nc][t] = gid;
+                nc++;
+                nacc++;
+                if (T < tthr) {
+                    done = true;
+                    break;
+                }
+            }
+            if (!done) {
+                if (st.ncand > st.kcount) {
+                    // resume after the last key looked at; entries at or below the active pass
+                    // threshold would be dropped anyway, so skip them at the traversal
+                    unsigned long long r = last_key;
+                    const bool exact = pass > 0 || slots == kPassSlots;
+                    if (exact) {
+                        const float thr = slots == kPassSlots ? fmaxf(last_d, tmin_sel) : tmin_sel;
+                        const unsigned long long skip = ((unsigned long long)f2h_bits(thr) << 48) | 0xFFFFFFFFFFFFull;
+                        r = skip > r ? skip : r;
+                    }
+                    st.resume = r;
+                    st.has_resume = true;
+                    if (++traversals > kMaxTraversals) {
+                        raise_status(a.status, GRAY_STATUS_STACK_OVERFLOW);
+                        done = true;
+                    }
+                } else {
+                    done = true;
+                }
+            }
+        }
+        // ---------------- backward hit list segment (warp aggregated) ----------------
+        if (grads) {
+            const uint32_t need = nc > 0 ? (uint32_t)nc + 2u : 0u;
+            uint32_t incl = need;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                uint32_t v = __shfl_up_sync(kFull, incl, off);
+                if (lane >= off) incl += v;
+            }
+            const uint32_t total = __shfl_sync(kFull, incl, 31);
+            uint32_t base = 0;
+            if (total > 0) {
+                if (lane == 31) base = atomicAdd(a.counter, total);
+                base = __shfl_sync(kFull, base, 31);
+            }
+            if (need > 0) {
+                const uint32_t off = base + incl - need;
+                const bool fits = base <= a.pool_size && total <= a.pool_size - base;
+                if (fits) {
+                    a.pool[off] = head;
+                    a.pool[off + 1] = (uint32_t)nc;
+                    for (int j = 0; j < nc; j++) a.pool[off + 2 + j] = (uint32_t)kbuf[j][threadIdx.x];
+                    head = off;
+                } else {
+                    raise_status(a.status, GRAY_STATUS_HITLIST_OVERFLOW);
+                }
+            }
+        }
+        first = false;
+    }
+
+    if (!inside) return;
+    if (!alive) {
+        a.head[pixel] = GRAY_NULL;  // inactive pixel: empty list, nothing else written
+        return;
+    }
+    // ---------------- truncated-tail estimate, background, write-out ----------------
+    const float rT = T - st.ft;
+    float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+    if (st.afx > 0) {
+        const float sa = __ll2float_rn(st.afx) * 0x1.0p-24f;
+        r0 = (__ll2float_rn(st.cfx0) * 0x1.0p-32f) / sa;
+        r1 = (__ll2float_rn(st.cfx1) * 0x1.0p-32f) / sa;
+        r2 = (__ll2float_rn(st.cfx2) * 0x1.0p-32f) / sa;
+    }
+    C0 = C0 + rT * r0;
+    C1 = C1 + rT * r1;
+    C2 = C2 + rT * r2;
+    if (render_depth) depth = depth / fmaxf(1.0f - T, *a.eps_fwd);
+    const float *bg = a.bg;
+    C0 = C0 + bg[0] * st.ft;
+    C1 = C1 + bg[1] * st.ft;
+    C2 = C2 + bg[2] * st.ft;
+    a.out_rgb[3 * pixel] = C0;
+    a.out_rgb[3 * pixel + 1] = C1;
+    a.out_rgb[3 * pixel + 2] = C2;
+    if (grads) {
+        a.out_depth[pixel] = depth;
+        a.out_T[pixel] = T;
+        a.out_fullT[pixel] = st.ft;
+        a.out_rem[3 * pixel] = r0;
+        a.out_rem[3 * pixel + 1] = r1;
+        a.out_rem[3 * pixel + 2] = r2;
+        a.ray_o[3 * pixel] = ro.x;
+        a.ray_o[3 * pixel + 1] = ro.y;
+        a.ray_o[3 * pixel + 2] = ro.z;
+        a.ray_d[3 * pixel] = rd.x;
+        a.ray_d[3 * pixel + 1] = rd.y;
+        a.ray_d[3 * pixel + 2] = rd.z;
+        a.stat_hit[pixel] += st.nhit;
+        a.stat_acc[pixel] += nacc;
+        a.head[pixel] = head;
+    } else {
+        const bool nro = *a.needs_ray_output != 0;
+        if (render_depth || nro) a.out_depth[pixel] = depth;
+        if (nro) {
+            a.ray_d[3 * pixel] = rd.x;
+            a.ray_d[3 * pixel + 1] = rd.y;
+            a.ray_d[3 * pixel + 2] = rd.z;
+        }
+        a.head[pixel] = GRAY_NULL;
+    }
+}
+
+cudaError_t launch_trace_forward(const gray_params &p, cudaStream_t s) {
+    FwdArgs a;
+    a.alloc_w = p.image_width;
+    a.render_w = p.render_width;
+    a.render_h = p.render_height;
+    a.n = p.gaussians.count;
+    a.cam_origin = p.camera.origin;
+    a.fov = p.camera.vertical_fov_radians;
+    a.w2c = p.camera.rotation_w2c;
+    a.znear = p.camera.znear;
+    a.zfar = p.camera.zfar;
+    a.exp_power = p.config.exp_power;
+    a.alpha_threshold = p.config.alpha_threshold;
+    a.t_threshold = p.config.t_threshold;
+    a.eps_fwd = p.config.eps_forward_normalization;
+    a.bg = p.config.background_channels;
+    a.render_depth = p.config.render_depth;
+    a.needs_ray_output = p.config.needs_ray_output;
+    a.rays_from_python = p.config.rays_from_python;
+    a.jitter = p.config.jitter_primary_rays;
+    a.grads_enabled = p.metadata.grads_enabled;
+    a.total_num_calls = p.metadata.total_num_calls;
+    a.geom = reinterpret_cast<const float4 *>(p.scene.geom);
+    a.live = reinterpret_cast<const float2 *>(p.scene.live);
+    a.channels = p.gaussians.channels;
+    a.nodes = reinterpret_cast<const float4 *>(p.scene.nodes);
+    a.root_box = p.scene.root_box;
+    a.out_rgb = p.framebuffer.output_channels;
+    a.out_depth = p.framebuffer.output_depth;
+    a.out_T = p.framebuffer.transmittance;
+    a.out_fullT = p.framebuffer.full_transmittance;
+    a.out_rem = p.framebuffer.remaining_channels_estimate;
+    a.ray_o = p.framebuffer.ray_origin;
+    a.ray_d = p.framebuffer.ray_direction;
+    a.stat_hit = p.stats.num_gaussians_hit;
+    a.stat_acc = p.stats.num_gaussians_accumulated;
+    a.head = p.hitlist.head_per_pixel;
+    a.counter = p.hitlist.total_words;
+    a.pool = p.hitlist.pool;
+    a.pool_size = p.hitlist.size;
+    a.status = p.status;
+    dim3 grid((p.render_width + kBlockW - 1) / kBlockW, (p.render_height + kBlockH - 1) / kBlockH);
+    trace_forward_kernel<kPassSlots><<<grid, kFwdThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Backward
+// ---------------------------------------------------------------------------------------------
+struct BwdArgs {
+    uint32_t alloc_w, render_w, render_h;
+    int n;
+    const float *exp_power, *alpha_threshold, *eps_scale_grad, *bg;
+    const float4 *geom, *l2w;
+    const float2 *live;
+    const float *scale, *channels;
+    const float4 *rotation;
+    const float *pix_T, *pix_fullT, *pix_rem, *ray_o, *ray_d, *grad_out;
+    const uint32_t *head, *pool;
+    uint32_t pool_size;
+    float *grad_acc;
+    int32_t *status;
+};
+
+__device__ __forceinline__ void red_add4(float *addr, float x, float y, float z, float w) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(x), "f"(y), "f"(z), "f"(w)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(128) trace_backward_kernel(const BwdArgs a) {
+    const int px = blockIdx.x * 16 + (threadIdx.x & 15);
+    const int py = blockIdx.y * 8 + (threadIdx.x >> 4);
+    if (px >= (int)a.render_w || py >= (int)a.render_h) return;
+    const uint32_t pixel = (uint32_t)py * a.alloc_w + (uint32_t)px;
+    uint32_t seg = a.head[pixel];
+    if (seg == GRAY_NULL) return;
+    const float pw = *a.exp_power, eps_sg = *a.eps_scale_grad;
+    const float Tfin = a.pix_T[pixel], fT = a.pix_fullT[pixel];
+    const f3 rem = mk3(a.pix_rem[3 * pixel], a.pix_rem[3 * pixel + 1], a.pix_rem[3 * pixel + 2]);
+    const f3 ro = mk3(a.ray_o[3 * pixel], a.ray_o[3 * pixel + 1], a.ray_o[3 * pixel + 2]);
+    const f3 rd = mk3(a.ray_d[3 * pixel], a.ray_d[3 * pixel + 1], a.ray_d[3 * pixel + 2]);
+    const f3 gout = mk3(a.grad_out[3 * pixel], a.grad_out[3 * pixel + 1], a.grad_out[3 * pixel + 2]);
+    const f3 bg = mk3(a.bg[0], a.bg[1], a.bg[2]);
+    const float dbg = dot3(bg, gout), drem = dot3(rem, gout);
+    const float npix = (float)(a.render_w * a.render_h);
+    float gT = 0.0f, T = Tfin;
+    int guard = 0;
+    while (seg != GRAY_NULL) {
+        if (seg + 2u > a.pool_size || ++guard > kPassSlots * kMaxPasses + 1) {
+            raise_status(a.status, GRAY_STATUS_HITLIST_OVERFLOW);
+            return;
+        }
+        const uint32_t prev = a.pool[seg], cnt = a.pool[seg + 1];
+        if (cnt > a.pool_size - seg - 2u) {
+            raise_status(a.status, GRAY_STATUS_HITLIST_OVERFLOW);
+            return;
+        }
+        for (int e = (int)cnt - 1; e >= 0; e--) {
+            const uint32_t gid = a.pool[seg + 2 + e];
+            if (gid >= (uint32_t)a.n) continue;
+            const float4 g0 = a.geom[3 * gid], g1 = a.geom[3 * gid + 1], g2 = a.geom[3 * gid + 2];
+            const float4 L0 = a.l2w[3 * gid], L1 = a.l2w[3 * gid + 1], L2 = a.l2w[3 * gid + 2];
+            const float2 lv = a.live[gid];
+            const float o = lv.x, sf = lv.y;
+            const f3 s = mk3(gexp(a.scale[3 * gid]), gexp(a.scale[3 * gid + 1]), gexp(a.scale[3 * gid + 2]));
+            const float4 qr = a.rotation[gid];
+            const float qlen = sqrtf(qr.x * qr.x + qr.y * qr.y + qr.z * qr.z + qr.w * qr.w);
+            const float qw = qr.x / qlen, qx = qr.y / qlen, qy = qr.z / qlen, qz = qr.w / qlen;
+            const f3 c = mk3(a.channels[3 * gid], a.channels[3 * gid + 1], a.channels[3 * gid + 2]);
+
+            LocalHit h;
+            local_ray(g0, g1, g2, ro, rd, h);
+            closest_point(h);
+            const f3 x = mk3((h.lo.x + h.s * h.dn.x) * sf, (h.lo.y + h.s * h.dn.y) * sf, (h.lo.z + h.s * h.dn.z) * sf);
+            const float sq = dot3(x, x);
+            const float gv = eval_gaussian(sq, pw);
+            const float alpha = maxalpha_mul(gv, o);
+
+            const float om = 1.0f - alpha;
+            const float w = T / om * alpha;
+            const float dgc = dot3(gout, c);
+            float ga = (dgc - gT) * T / om;
+            ga = ga + -fT / om * dbg;
+            ga = ga + -((Tfin - fT) / om) * drem;
+            gT = gT + (dgc - gT) * alpha;
+            float go = maxalpha_mul(ga, gv);
+            go = go * o * (1.0f - o);
+            const float ggv = maxalpha_mul(ga, o);
+            float gsq;
+            if (pw == 1.0f) gsq = gv;
+            else if (pw == 2.0f) gsq = gv * sq;
+            else if (pw == 3.0f) gsq = gv * sq * sq;
+            else gsq = gv * gpow(sq, pw - 1.0f);
+            const f3 gxl = mk3(-x.x * gsq * ggv, -x.y * gsq * ggv, -x.z * gsq * ggv);
+            const f3 gxw = mk3((g0.x * gxl.x + g1.x * gxl.y + g2.x * gxl.z) * sf,
+                               (g0.y * gxl.x + g1.y * gxl.y + g2.y * gxl.z) * sf,
+                               (g0.z * gxl.x + g1.z * gxl.y + g2.z * gxl.z) * sf);
+            // d loss / d L2W rows: -gxw_i * x
+            const f3 gl0 = mk3(-gxw.x * x.x, -gxw.x * x.y, -gxw.x * x.z);
+            const f3 gl1 = mk3(-gxw.y * x.x, -gxw.y * x.y, -gxw.y * x.z);
+            const f3 gl2 = mk3(-gxw.z * x.x, -gxw.z * x.y, -gxw.z * x.z);
+            const f3 den = mk3(s.x * sf + eps_sg, s.y * sf + eps_sg, s.z * sf + eps_sg);
+            const f3 gs = mk3((gl0.x * (L0.x / den.x) + gl1.x * (L1.x / den.x) + gl2.x * (L2.x / den.x)) * s.x,
+                              (gl0.y * (L0.y / den.y) + gl1.y * (L1.y / den.y) + gl2.y * (L2.y / den.y)) * s.y,
+                              (gl0.z * (L0.z / den.z) + gl1.z * (L1.z / den.z) + gl2.z * (L2.z / den.z)) * s.z);
+            // rotation-matrix gradient and its pull-back to the (normalised) quaternion
+            const float r00 = gl0.x * s.x, r01 = gl0.y * s.y, r02 = gl0.z * s.z;
+            const float r10 = gl1.x * s.x, r11 = gl1.y * s.y, r12 = gl1.z * s.z;
+            const float r20 = gl2.x * s.x, r21 = gl2.y * s.y, r22 = gl2.z * s.z;
+            const float g_r = 2.0f * qx * (r21 - r12) + 2.0f * qy * (r02 - r20) + 2.0f * qz * (r10 - r01);
+            const float g_x = -4.0f * qx * (r11 + r22) + 2.0f * qy * (r01 + r10) + 2.0f * qz * (r02 + r20) +
+                              2.0f * qw * (r21 - r12);
+            const float g_y = 2.0f * qx * (r01 + r10) - 4.0f * qy * (r00 + r22) + 2.0f * qz * (r12 + r21) +
+                              2.0f * qw * (r02 - r20);
+            const float g_z = 2.0f * qx * (r02 + r20) + 2.0f * qy * (r12 + r21) - 4.0f * qz * (r00 + r11) +
+                              2.0f * qw * (r10 - r01);
+            const float dq = g_r * qr.x + g_x * qr.y + g_y * qr.z + g_z * qr.w;
+            const float l3 = qlen * qlen * qlen;
+            float *acc = a.grad_acc + 16 * (size_t)gid;
+            red_add4(acc, dq * -qr.x / l3 + g_r / qlen, dq * -qr.y / l3 + g_x / qlen, dq * -qr.z / l3 + g_y / qlen,
+                     dq * -qr.w / l3 + g_z / qlen);
+            red_add4(acc + 4, -gxw.x, -gxw.y, -gxw.z, go);
+            red_add4(acc + 8, gs.x, gs.y, gs.z, w / npix);
+            red_add4(acc + 12, gout.x * w, gout.y * w, gout.z * w, 1.0f);
+            T = T / om;
+        }
+        seg = prev;
+    }
+}
+
+cudaError_t launch_trace_backward(const gray_params &p, cudaStream_t s) {
+    BwdArgs a;
+    a.alloc_w = p.image_width;
+    a.render_w = p.render_width;
+    a.render_h = p.render_height;
+    a.n = p.gaussians.count;
+    a.exp_power = p.config.exp_power;
+    a.alpha_threshold = p.config.alpha_threshold;
+    a.eps_scale_grad = p.config.eps_scale_grad;
+    a.bg = p.config.background_channels;
+    a.geom = reinterpret_cast<const float4 *>(p.scene.geom);
+    a.l2w = reinterpret_cast<const float4 *>(p.scene.l2w);
+    a.live = reinterpret_cast<const float2 *>(p.scene.live);
+    a.scale = p.gaussians.scale;
+    a.channels = p.gaussians.channels;
+    a.rotation = reinterpret_cast<const float4 *>(p.gaussians.rotation);
+    a.pix_T = p.framebuffer.transmittance;
+    a.pix_fullT = p.framebuffer.full_transmittance;
+    a.pix_rem = p.framebuffer.remaining_channels_estimate;
+    a.ray_o = p.framebuffer.ray_origin;
+    a.ray_d = p.framebuffer.ray_direction;
+    a.grad_out = p.framebuffer.grad_output_channels;
+    a.head = p.hitlist.head_per_pixel;
+    a.pool = p.hitlist.pool;
+    a.pool_size = p.hitlist.size;
+    a.grad_acc = p.scene.grad_acc;
+    a.status = p.status;
+    dim3 grid((p.render_width + 15) / 16, (p.render_height + 7) / 8);
+    trace_backward_kernel<<<grid, 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace gray

@@ -1,0 +1,197 @@
+/*
+ * gray_gb300.h -- C ABI of the GB300-native Gaussian ray tracer (libgray_gb300.so).
+ *
+ * The library replaces the OptiX path behind GRay's torch binding
+ * (graphdeco-inria/gray: cuda/raytracer.cpp:3-13 registers torch.classes.gray.Raytracer,
+ * whose methods are defined in cuda/raytracer.h:88-149).  Every entry point here is one of
+ * those methods, taking the same state the reference keeps in its `Params` block
+ * (cuda/params.h:12-31): plain device pointers owned by the caller, image and scene sizes,
+ * and the CUDA stream to run on.  No torch types cross this boundary.
+ *
+ * Conventions
+ *  - All pointers in the structs are device pointers unless stated otherwise.  Runtime knobs
+ *    are one-element device arrays read by the kernels, exactly like the reference's
+ *    ConfigDataHolder tensors (cuda/core/config.h:5-22), so they can change without a host
+ *    round trip.
+ *  - `stream` is a cudaStream_t passed as void*; 0 selects the legacy default stream.
+ *  - Return value: GRAY_OK or a GRAY_ERR_* code; gray_last_error() gives the message.
+ *    Conditions that only the device can detect (hit-list overflow, traversal-stack overflow,
+ *    an exhausted spin budget) are OR-ed into `*status` (a device int32) instead of trapping;
+ *    the host reads it after synchronising.
+ *  - Layouts follow the reference holders (cuda/core/gaussians.h:70-160): mean [N,3],
+ *    rotation [N,4] (r,x,y,z, unnormalised), scale [N,3] (log), opacity [N,1] (logit),
+ *    channels [N,3], sh_coeffs_dc [N,1,3], sh_coeffs_rest [N,K,3] (fp32, or fp16 when
+ *    sh_is_fp16), framebuffer arrays [H_alloc, W_alloc, C].
+ */
+#ifndef GRAY_GB300_H
+#define GRAY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GRAY_OK 0
+#define GRAY_ERR_INVALID_ARGUMENT 1
+#define GRAY_ERR_CUDA 2
+#define GRAY_ERR_OUT_OF_RANGE 3
+
+/* bits of the device status word */
+#define GRAY_STATUS_HITLIST_OVERFLOW 1    /* backward hit list full (reference: PPLL overflow __trap) */
+#define GRAY_STATUS_STACK_OVERFLOW 2      /* BVH traversal stack exhausted */
+#define GRAY_STATUS_REFIT_TIMEOUT 4       /* bottom-up refit spin budget exhausted */
+
+/* Gaussian parameters and optimiser state (cuda/core/gaussians.h:7-65). */
+typedef struct gray_gaussians {
+    int32_t count;
+    int32_t max_sh_degree;
+    int32_t num_sh_coeffs;        /* (max_sh_degree + 1)^2 - 1 */
+    int32_t sh_is_fp16;           /* inference_only: SH stored as binary16 */
+    int32_t *current_sh_degree;   /* [1] */
+
+    float *mean, *rotation, *scale, *opacity, *channels;
+    void *sh_coeffs_dc, *sh_coeffs_rest;
+
+    float *lr_mean, *lr_rotation, *lr_scale, *lr_opacity, *lr_channels, *lr_sh_dc, *lr_sh_rest; /* [0] read */
+    float *beta_1, *beta_2, *epsilon;
+    int32_t *sh_update_laziness;
+
+    float *grad_mean, *grad_rotation, *grad_scale, *grad_opacity, *grad_channels, *grad_sh_coeffs_dc,
+        *grad_sh_coeffs_rest;
+    float *first_moment_mean, *first_moment_rotation, *first_moment_scale, *first_moment_opacity,
+        *first_moment_channels, *first_moment_sh_coeffs_dc, *first_moment_sh_coeffs_rest;
+    float *second_moment_mean, *second_moment_rotation, *second_moment_scale, *second_moment_opacity,
+        *second_moment_channels, *second_moment_sh_coeffs_dc, *second_moment_sh_coeffs_rest;
+
+    float *pruning_weight;
+    int32_t *pruning_counter;
+    uint8_t *was_visible;
+    float *marked;
+} gray_gaussians;
+
+/* Pinhole camera (cuda/core/camera.h:8-15); rotation_w2c rows are the c2w columns. */
+typedef struct gray_camera {
+    float *origin;               /* [3] */
+    float *vertical_fov_radians; /* [1] */
+    float *rotation_c2w;         /* [3,3] */
+    float *rotation_w2c;         /* [3,3] */
+    float *znear, *zfar;         /* [1] each */
+} gray_camera;
+
+/* Runtime knobs (cuda/core/config.h:5-22); every field is a one-element device array. */
+typedef struct gray_config {
+    float *exp_power, *alpha_threshold, *t_threshold;
+    uint8_t *jitter_primary_rays;
+    float *global_scale_factor, *eps_forward_normalization, *eps_scale_grad;
+    float *background_channels; /* [3] */
+    uint8_t *render_depth, *render_ellipsoids;
+    float *ellipsoid_min_opacity;
+    uint8_t *rays_from_python, *zero_grads, *enable_sh, *needs_ray_output, *update_channels;
+} gray_config;
+
+/* Per-pixel outputs and saved state (cuda/core/framebuffer.h:22-31). */
+typedef struct gray_framebuffer {
+    float *output_channels;            /* [H,W,3] */
+    float *output_depth;               /* [H,W,1] */
+    float *transmittance;              /* [H,W,1] */
+    float *full_transmittance;         /* [H,W,1] */
+    float *remaining_channels_estimate;/* [H,W,3] */
+    float *ray_origin, *ray_direction; /* [H,W,3] */
+    float *grad_output_channels;       /* [H,W,3] */
+} gray_framebuffer;
+
+/* cuda/core/metadata.h:3-10 */
+typedef struct gray_metadata {
+    uint8_t *run_forward_pass, *run_backward_pass, *grads_enabled;
+    uint32_t *total_num_calls, *total_num_steps;
+} gray_metadata;
+
+/* cuda/core/stats.h:3-6 (per-pixel counters, accumulated while grads are enabled) */
+typedef struct gray_stats {
+    int32_t *num_gaussians_hit, *num_gaussians_accumulated;
+} gray_stats;
+
+/* Backward hit list (replaces the reference's backward per-pixel linked list,
+ * cuda/core/per_pixel_linked_list.h:5-62).  Composited gaussian ids are stored per pixel as
+ * a chain of segments [prev_segment, count, id_0 .. id_{count-1}] in `pool` (u32 words);
+ * head_per_pixel holds the newest segment of each pixel (0xFFFFFFFF = none). */
+typedef struct gray_hitlist {
+    uint32_t *head_per_pixel; /* [H_alloc * W_alloc] */
+    uint32_t *total_words;    /* [1] bump counter */
+    uint32_t *pool;           /* [size] */
+    uint32_t size;
+} gray_hitlist;
+
+/* Scene-side workspace owned by the caller (sizes from gray_scene_workspace_sizes). */
+typedef struct gray_scene {
+    float *geom;        /* [N,12] snapshot rows (M | mu), M = diag(1/s) R^T          */
+    float *l2w;         /* [N,12] snapshot rows of R diag(s)                          */
+    float *aabb;        /* [N,8]  leaf boxes (min xyz, pad, max xyz, pad)             */
+    uint8_t *visible;   /* [N]    snapshot visibility (populate_bvh_kernel mask)      */
+    float *live;        /* [N,2]  per-forward (sigmoid(opacity), scaling factor)      */
+    float *grad_acc;    /* [N,16] backward accumulators, zero between passes          */
+    float *nodes;       /* [max(N-1,1),16] BVH2 nodes: child boxes + child links      */
+    int32_t *int_parent;  /* [max(N-1,1)] */
+    int32_t *leaf_parent; /* [N] indexed by sorted leaf position */
+    uint32_t *order;      /* [N] sorted leaf position -> gaussian id */
+    uint32_t *codes;      /* [N] Morton codes in sorted order */
+    uint32_t *refit_flags;/* [max(N-1,1)] */
+    uint32_t *sort_tmp;   /* [sort_tmp_words] */
+    float *root_box;      /* [8] */
+    uint32_t *bounds;     /* [8] order-preserving encoded scene bounds (scratch) */
+    int32_t bvh_valid;    /* host flag: a rebuild has been done for this count */
+} gray_scene;
+
+typedef struct gray_params {
+    uint32_t image_width, image_height;   /* allocated framebuffer */
+    uint32_t render_width, render_height; /* active top-left rectangle (set_render_resolution) */
+    gray_camera camera;
+    gray_config config;
+    gray_framebuffer framebuffer;
+    gray_gaussians gaussians;
+    gray_metadata metadata;
+    gray_stats stats;
+    gray_hitlist hitlist;
+    gray_scene scene;
+    int32_t *status; /* device int32, GRAY_STATUS_* bits */
+} gray_params;
+
+/* Workspace sizes in 32-bit words for n Gaussians: sort_tmp_words. */
+size_t gray_sort_tmp_words(int32_t n);
+
+/* Raytracer::forward_pass (cuda/raytracer.h:88-102): counts the call, resets the backward
+ * hit list and was_visible, evaluates SH colours (if enable_sh) and traces the render
+ * rectangle.  grads_enabled must have been set by the caller (MetaDataHolder::update). */
+int gray_forward_pass(const gray_params *p, void *stream);
+
+/* Raytracer::forward_pass_display (cuda/raytracer.h:104-114): SH + trace, no resets. */
+int gray_forward_pass_display(const gray_params *p, void *stream);
+
+/* Raytracer::backward_pass (cuda/raytracer.h:116-124): reverse replay of the hit lists into the
+ * gradient arrays (and pruning_weight, was_visible), then the SH backward. */
+int gray_backward_pass(const gray_params *p, void *stream);
+
+/* Raytracer::step (cuda/raytracer.h:126-133 -> cuda/opt/adam.cu:70-83): total_num_steps += 1
+ * and one fused Adam step over all parameter groups (SH every sh_update_laziness steps). */
+int gray_step(const gray_params *p, void *stream);
+
+/* Raytracer::update_bvh (cuda/raytracer.h:135 -> cuda/optix/bvh_wrapper.h:25-39): snapshot the
+ * current parameters into the instance records and refit the hierarchy's boxes. */
+int gray_update_bvh(const gray_params *p, void *stream);
+
+/* Raytracer::rebuild_bvh (cuda/raytracer.h:137-142 -> cuda/optix/bvh_wrapper.h:89-115): snapshot
+ * and full LBVH build (Morton codes, radix sort, Karras hierarchy, bottom-up boxes). */
+int gray_rebuild_bvh(const gray_params *p, void *stream);
+
+/* Message of the last error returned on the calling thread. */
+const char *gray_last_error(void);
+
+/* Library version string. */
+const char *gray_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

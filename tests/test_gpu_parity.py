@@ -1,0 +1,340 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.  Needs a GB300.
+
+Bar: integer/index results bit-exact (hit counts, composited gaussian id lists, BVH codes, order and
+nodes), the fp16-keyed compositing results bit-exact (transmittance T, tail estimate), values
+that depend on the order hits are found in (full transmittance, hence the final colour) within
+float32 rounding, and gradients (float atomics in arbitrary order) within 1e-4 relative.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from gray_gb300 import synthetic
+from tests import gpu_util as G
+
+pytestmark = pytest.mark.gpu
+
+RGB_TOL = 2e-6        # colour: order of the full-transmittance product only
+GRAD_RTOL = 1e-4      # gradients: fp32 atomics vs the oracle's double accumulation
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda(gray_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _grad_close(gpu, ref, rtol=GRAD_RTOL):
+    scale = max(float(np.abs(ref).max()), 1e-12)
+    assert np.abs(gpu - ref).max() <= rtol * scale + 1e-9, (np.abs(gpu - ref).max(), scale)
+
+
+def _compare_forward(rt, fwd, check_lists=True):
+    f = G.fb_numpy(rt)
+    st = rt.get_stats()
+    nhit = st.num_gaussians_hit.reshape(-1).cpu().numpy()
+    nacc = st.num_gaussians_accumulated.reshape(-1).cpu().numpy()
+    alive = fwd["nhit"] >= 0
+    assert np.array_equal(nhit[alive], fwd["nhit"][alive])
+    assert np.array_equal(nacc[alive], fwd["nacc"][alive])
+    assert np.array_equal(f["transmittance"][alive, 0], fwd["T"][alive])
+    assert np.array_equal(f["remaining_channels_estimate"][alive], fwd["rem"][alive])
+    assert np.allclose(f["full_transmittance"][alive, 0], fwd["fullT"][alive], rtol=2e-6, atol=1e-7)
+    assert np.abs(f["output_channels"][alive] - fwd["rgb"][alive]).max() < RGB_TOL
+    if check_lists:
+        gl, ol = G.hit_lists(rt), G.oracle_lists(fwd)
+        for i in np.nonzero(alive)[0]:
+            assert np.array_equal(gl[i], ol[i]), i
+
+
+def _oracle_scene(O, mean, rot, scale, opac, a_thr=0.01, p=2.0):
+    geom, l2w, aabb, vis = O.snapshot(mean, rot, scale, np.asarray(opac).reshape(-1), a_thr, p)
+    live = O.forward_prep(np.asarray(opac).reshape(-1), a_thr, p)
+    return geom, l2w, aabb, vis, live
+
+
+NAMES = ["single_a0.01", "single_a0.3", "multi_t0.0", "multi_t0.5"]
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_reference_scenes_forward_backward(oracle, golden, name):
+    p = name + "_"
+    a_thr, t_thr = float(golden[p + "alpha_threshold"]), float(golden[p + "t_threshold"])
+    rt = G.make_tracer(32, 32, golden[p + "mean"], golden[p + "rotation"], golden[p + "log_scale"],
+                       golden[p + "logit_opacity"], channels=golden[p + "color"], alpha_threshold=a_thr,
+                       t_threshold=t_thr, bg=tuple(golden[p + "bg"]))
+    G.trace_rays(rt, golden["rays_o"], golden["rays_d"])
+    geom, l2w, aabb, vis, live = _oracle_scene(oracle, golden[p + "mean"], golden[p + "rotation"],
+                                               golden[p + "log_scale"], golden[p + "logit_opacity"], a_thr)
+    cfg = oracle.TraceConfig(alpha_threshold=a_thr, t_threshold=t_thr, bg=tuple(golden[p + "bg"]))
+    fwd = oracle.trace_forward(golden["rays_o"], golden["rays_d"], geom, live, golden[p + "color"], vis, cfg)
+    _compare_forward(rt, fwd)
+    img = G.fb_numpy(rt)["output_channels"]
+    assert np.abs(img - golden[p + "ref64_rgb"]).max() < 3e-4  # fp16-alpha bound vs the FP64 test loop
+
+    gout = golden[p + "ref64_grad_out"]
+    rt.get_framebuffer().grad_output_channels.copy_(torch.from_numpy(gout).reshape(32, 32, 3))
+    rt.backward_pass()
+    torch.cuda.synchronize()
+    rt.check_status()
+    ref = oracle.trace_backward(32, 32, golden["rays_o"], golden["rays_d"], fwd, gout, geom, l2w,
+                                golden[p + "logit_opacity"], golden[p + "log_scale"], golden[p + "rotation"],
+                                golden[p + "color"], cfg)
+    g = rt.get_gaussians()
+    got = {"rotation": g.grad_rotation, "mean": g.grad_mean, "logit_opacity": g.grad_opacity,
+           "log_scale": g.grad_scale, "color": g.grad_channels}
+    sl = {"rotation": slice(0, 4), "mean": slice(4, 7), "logit_opacity": slice(7, 8), "log_scale": slice(8, 11),
+          "color": slice(12, 15)}
+    for k, t in got.items():
+        t = t.cpu().numpy()
+        _grad_close(t, ref[:, sl[k]])
+        assert np.abs(t - golden[p + "ref64_grad_" + k]).max() < 1e-4, k  # reference tests' tolerance
+    assert np.allclose(g.pruning_weight.cpu().numpy()[:, 0], ref[:, 11], rtol=1e-5, atol=1e-12)
+    assert np.array_equal(g.was_visible.cpu().numpy()[:, 0], ref[:, 15] > 0)
+
+
+def test_snapshot_and_bvh_bit_exact(oracle):
+    sc = synthetic.clustered_scene(30_000, seed=3)
+    rt = G.make_tracer(16, 16, sc.mean, sc.rotation, sc.scale, sc.opacity, channels=np.zeros((sc.n, 3), np.float32))
+    geom, l2w, aabb, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, sc.scale, sc.opacity)
+    ws = rt.scene_workspace()
+    assert np.array_equal(ws.geom.cpu().numpy(), geom)
+    assert np.array_equal(ws.l2w.cpu().numpy(), l2w)
+    assert np.array_equal(ws.aabb.cpu().numpy(), aabb)
+    assert np.array_equal(ws.visible.cpu().numpy(), vis)
+    tree = oracle.Bvh(aabb, vis)
+    assert np.array_equal(ws.codes.cpu().numpy().view(np.uint32), tree.codes)
+    assert np.array_equal(ws.order.cpu().numpy().view(np.uint32), tree.order)
+    assert np.array_equal(ws.nodes.cpu().numpy(), tree.nodes)
+    assert np.array_equal(ws.root_box.cpu().numpy(), tree.root_box)
+    # refit after moving the Gaussians keeps the topology and matches the oracle's refit
+    g = rt.get_gaussians()
+    with torch.no_grad():
+        g.mean.add_(0.01)
+        g.scale.add_(0.1)
+    rt.update_bvh()
+    torch.cuda.synchronize()
+    _, _, aabb2, vis2 = oracle.snapshot(sc.mean + np.float32(0.01), sc.rotation, sc.scale + np.float32(0.1),
+                                        sc.opacity[:, 0])
+    tree.refit(aabb2)
+    assert np.array_equal(ws.aabb.cpu().numpy(), aabb2)
+    assert np.array_equal(ws.nodes.cpu().numpy(), tree.nodes)
+    assert np.array_equal(ws.root_box.cpu().numpy(), tree.root_box)
+
+
+def _camera_rays_gpu(rt, cam):
+    rt.get_camera().znear.fill_(0.0)
+    rt.get_camera().zfar.fill_(99999.9)
+    rt.get_camera().vertical_fov_radians.fill_(cam.fov_y)
+    rt.get_camera().set_pose(cam.origin_cuda(), cam.rotation_c2w_blender_cuda())
+    rt.get_config().rays_from_python.fill_(False)
+    with torch.enable_grad():
+        rt.forward_pass()
+    torch.cuda.synchronize()
+    f = G.fb_numpy(rt)
+    return f["ray_origin"], f["ray_direction"]
+
+
+def test_small_scene_sh_camera_and_passes(oracle):
+    """64 Gaussians, SH degree 3, one 256x256 camera at distance 4; 16-slot passes are the
+    reference's 32 (its BUFFER_SIZE); camera rays checked against the oracle's camera."""
+    sc = synthetic.small_scene(seed=0)
+    cam = synthetic.camera_small()
+    rt = G.make_tracer(256, 256, sc.mean, sc.rotation, sc.scale, sc.opacity, sh_dc=sc.sh_dc, sh_rest=sc.sh_rest,
+                       sh_degree=3)
+    ro, rd = _camera_rays_gpu(rt, cam)
+    oro, ord_ = oracle.camera_rays(256, 256, cam.fov_y, cam.origin.astype(np.float32), cam.rotation_c2w_blender())
+    assert np.abs(rd - ord_).max() < 1e-6 and np.abs(ro - oro).max() == 0
+    chan = oracle.sh_forward(3, sc.mean, cam.origin.astype(np.float32), sc.sh_dc[:, 0, :], sc.sh_rest)
+    assert np.array_equal(rt.get_gaussians().channels.cpu().numpy(), chan)
+    geom, l2w, aabb, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, sc.scale, sc.opacity)
+    cfg = oracle.TraceConfig(t_threshold=0.03)
+    fwd = oracle.trace_forward(ro, rd, geom, live, chan, vis, cfg)
+    _compare_forward(rt, fwd)
+    assert fwd["nhit"].sum() > 1000
+
+    rng = np.random.default_rng(5)
+    gout = rng.standard_normal((256 * 256, 3)).astype(np.float32)
+    rt.get_framebuffer().grad_output_channels.copy_(torch.from_numpy(gout).reshape(256, 256, 3))
+    rt.backward_pass()
+    torch.cuda.synchronize()
+    rt.check_status()
+    ref = oracle.trace_backward(256, 256, ro, rd, fwd, gout, geom, l2w, sc.opacity, sc.scale, sc.rotation, chan, cfg)
+    g = rt.get_gaussians()
+    _grad_close(g.grad_rotation.cpu().numpy(), ref[:, 0:4])
+    _grad_close(g.grad_opacity.cpu().numpy(), ref[:, 7:8])
+    _grad_close(g.grad_scale.cpu().numpy(), ref[:, 8:11])
+    _grad_close(g.grad_channels.cpu().numpy(), ref[:, 12:15])
+    # SH backward on the accumulated colour gradient, then mean gradient = trace + SH parts
+    vis_b = (ref[:, 15] > 0).astype(np.uint8)
+    gdc, grest, gmean = oracle.sh_backward(3, sc.mean, cam.origin.astype(np.float32), sc.sh_rest, chan,
+                                           g.grad_channels.cpu().numpy(), vis_b, ref[:, 4:7].astype(np.float32))
+    _grad_close(g.grad_sh_coeffs_dc.cpu().numpy().reshape(-1, 3), gdc)
+    _grad_close(g.grad_sh_coeffs_rest.cpu().numpy(), grest)
+    _grad_close(g.grad_mean.cpu().numpy(), gmean)
+
+
+def test_multipass_selection_and_segments(oracle):
+    """Many faint Gaussians on the same rays with t_threshold = 0: rays composite hundreds of hits,
+    crossing many 32-slot passes; the hit list chains one segment per traversal."""
+    rng = np.random.default_rng(11)
+    n = 3000
+    mean = np.stack([rng.normal(0, 0.15, n), rng.normal(0, 0.15, n), rng.uniform(-3, 3, n)], 1).astype(np.float32)
+    rot = rng.standard_normal((n, 4)).astype(np.float32)
+    scale = np.full((n, 3), math.log(0.3), np.float32)
+    opac = np.full((n, 1), -2.5, np.float32)  # sigmoid ~ 0.076
+    chan = rng.uniform(0, 1, (n, 3)).astype(np.float32)
+    W = H = 24
+    rt = G.make_tracer(W, H, mean, rot, scale, opac, channels=chan, t_threshold=0.0, bg=(0.2, 0.3, 0.4))
+    cam_o = np.array([0.0, 0.0, 6.0], np.float32)
+    ys, xs = np.meshgrid(np.linspace(-0.08, 0.08, H), np.linspace(-0.08, 0.08, W), indexing="ij")
+    d = np.stack([xs.ravel(), ys.ravel(), -np.ones(W * H)], 1)
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    o = np.repeat(cam_o[None], W * H, 0)
+    G.trace_rays(rt, o, d)
+    geom, l2w, aabb, vis, live = _oracle_scene(oracle, mean, rot, scale, opac)
+    cfg = oracle.TraceConfig(t_threshold=0.0, bg=(0.2, 0.3, 0.4))
+    fwd = oracle.trace_forward(o, d, geom, live, chan, vis, cfg)
+    assert fwd["nacc"].max() > 200
+    _compare_forward(rt, fwd)
+    gout = rng.standard_normal((W * H, 3)).astype(np.float32)
+    rt.get_framebuffer().grad_output_channels.copy_(torch.from_numpy(gout).reshape(H, W, 3))
+    rt.backward_pass()
+    torch.cuda.synchronize()
+    rt.check_status()
+    ref = oracle.trace_backward(W, H, o, d, fwd, gout, geom, l2w, opac, scale, rot, chan, cfg)
+    g = rt.get_gaussians()
+    _grad_close(g.grad_rotation.cpu().numpy(), ref[:, 0:4], 3e-4)
+    _grad_close(g.grad_mean.cpu().numpy(), ref[:, 4:7], 3e-4)
+    _grad_close(g.grad_channels.cpu().numpy(), ref[:, 12:15], 3e-4)
+
+
+def test_znear_zfar_and_render_rectangle(oracle):
+    sc = synthetic.gradcheck_scene(seed=2, n=400)
+    chan = np.random.default_rng(0).uniform(0, 1, (sc.n, 3)).astype(np.float32)
+    W, H = 48, 40
+    rt = G.make_tracer(W, H, sc.mean, sc.rotation, sc.scale, sc.opacity, channels=chan, render_depth=True)
+    cam = synthetic.look_at((0.3, -5.0, 0.4), (0, 0, 0), (0, 0, 1), 0.9, W, H)
+    rt.get_camera().znear.fill_(4.2)
+    rt.get_camera().zfar.fill_(6.1)
+    rt.get_camera().vertical_fov_radians.fill_(cam.fov_y)
+    rt.get_camera().set_pose(cam.origin_cuda(), cam.rotation_c2w_blender_cuda())
+    rt.set_render_resolution(40, 33)
+    rt.get_config().rays_from_python.fill_(False)
+    with torch.enable_grad():
+        rt.forward_pass()
+    torch.cuda.synchronize()
+    f = G.fb_numpy(rt)
+    geom, l2w, aabb, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, sc.scale, sc.opacity)
+    mask = np.zeros((H, W), bool)
+    mask[:33, :40] = True
+    idx = np.nonzero(mask.ravel())[0]
+    cfg = oracle.TraceConfig(znear=4.2, zfar=6.1, render_depth=True)
+    fwd = oracle.trace_forward(f["ray_origin"][idx], f["ray_direction"][idx], geom, live, chan, vis, cfg)
+    assert np.array_equal(f["transmittance"][idx, 0], fwd["T"])
+    assert np.array_equal(f["output_depth"][idx, 0], fwd["depth"])
+    assert np.abs(f["output_channels"][idx] - fwd["rgb"]).max() < RGB_TOL
+    lists = G.hit_lists(rt)
+    ol = G.oracle_lists(fwd)
+    for k, i in enumerate(idx):
+        assert np.array_equal(lists[i], ol[k])
+    assert all(len(lists[i]) == 0 for i in np.nonzero(~mask.ravel())[0])
+
+
+def test_inactive_pixels_and_empty_scene(oracle):
+    sc = synthetic.small_scene(seed=1, n=16)
+    chan = np.ones((sc.n, 3), np.float32)
+    rt = G.make_tracer(8, 8, sc.mean, sc.rotation, sc.scale, sc.opacity, channels=chan, bg=(0.5, 0.5, 0.5))
+    o = np.zeros((64, 3), np.float32)
+    o[:, 1] = -4
+    d = np.zeros((64, 3), np.float32)
+    d[:32, 1] = 1.0  # second half: zero direction = inactive pixel (cuda/shaders.cu:86-88)
+    rt.get_framebuffer().output_channels.fill_(-7.0)
+    G.trace_rays(rt, o, d)
+    f = G.fb_numpy(rt)
+    assert np.all(f["output_channels"][32:] == -7.0)
+    assert np.all(f["output_channels"][:32] != -7.0)
+    # every Gaussian pruned: the render is background only
+    rt.resize(0)
+    rt.rebuild_bvh()
+    G.trace_rays(rt, o, d)
+    f = G.fb_numpy(rt)
+    assert np.allclose(f["output_channels"][:32], 0.5)
+
+
+def test_hitlist_overflow_is_reported_not_trapped(oracle):
+    sc = synthetic.small_scene(seed=0)
+    cam = synthetic.camera_small(64, 64, 64.0)
+    rt = G.make_tracer(64, 64, sc.mean, sc.rotation, sc.scale, sc.opacity, channels=np.ones((sc.n, 3), np.float32),
+                       pool_words=16)
+    rt.get_camera().vertical_fov_radians.fill_(cam.fov_y)
+    rt.get_camera().set_pose(cam.origin_cuda(), cam.rotation_c2w_blender_cuda())
+    rt.get_camera().zfar.fill_(1e5)
+    with torch.enable_grad():
+        rt.forward_pass()
+    torch.cuda.synchronize()
+    from gray_gb300 import _lib
+
+    with pytest.raises(_lib.GrayError, match="overflow"):
+        rt.check_status()
+    # the context stays usable
+    rt.check_status()
+    assert torch.isfinite(rt.get_framebuffer().output_channels).all()
+
+
+def test_adam_step_bit_exact(oracle):
+    rng = np.random.default_rng(4)
+    n = 1037
+    rt = G.make_tracer(8, 8, rng.normal(0, 1, (n, 3)), rng.normal(0, 1, (n, 4)), rng.normal(-3, 0.3, (n, 3)),
+                       rng.normal(0, 1, (n, 1)), sh_dc=rng.normal(0.5, 0.2, (n, 1, 3)),
+                       sh_rest=rng.normal(0, 0.05, (n, 15, 3)), sh_degree=3)
+    g = rt.get_gaussians()
+    lrs = dict(channels=0.0025, opacity=0.025, mean=1.6e-4, rotation=1e-3, scale=5e-3, sh_dc=2.5e-3, sh_rest=1.25e-4)
+    st = {}
+    name_map = {"sh_dc": "sh_coeffs_dc", "sh_rest": "sh_coeffs_rest"}
+    with torch.no_grad():
+        for name in ("channels", "opacity", "mean", "rotation", "scale", "sh_dc", "sh_rest"):
+            t = name_map.get(name, name)
+            p = getattr(g, t)
+            for pre, scale in (("grad_", 0.1), ("first_moment_", 0.01), ("second_moment_", 0.0)):
+                v = torch.from_numpy(rng.normal(0, scale, tuple(p.shape)).astype(np.float32))
+                if pre == "second_moment_":
+                    v = torch.from_numpy(np.abs(rng.normal(0, 1e-3, tuple(p.shape))).astype(np.float32))
+                getattr(g, pre + t).copy_(v)
+            getattr(g, "lr_" + name).fill_(lrs[name])
+            st[name] = p.detach().cpu().numpy().reshape(-1).copy()
+            st["g_" + name] = getattr(g, "grad_" + t).cpu().numpy().reshape(-1).copy()
+            st["m_" + name] = getattr(g, "first_moment_" + t).cpu().numpy().reshape(-1).copy()
+            st["v_" + name] = getattr(g, "second_moment_" + t).cpu().numpy().reshape(-1).copy()
+    cfg = rt.get_config()
+    cfg.zero_grads.fill_(True)
+    cfg.update_channels.fill_(False)
+    rt.get_metadata().total_num_steps.fill_(6)
+    rt.step()  # step becomes 7
+    torch.cuda.synchronize()
+    oracle.adam_step(st, lrs, n, 15, 7, zero_grads=True, update_channels=False)
+    for name in ("channels", "opacity", "mean", "rotation", "scale", "sh_dc", "sh_rest"):
+        t = name_map.get(name, name)
+        assert np.array_equal(getattr(g, t).detach().cpu().numpy().reshape(-1), st[name]), name
+        assert np.array_equal(getattr(g, "first_moment_" + t).cpu().numpy().reshape(-1), st["m_" + name]), name
+        assert np.array_equal(getattr(g, "second_moment_" + t).cpu().numpy().reshape(-1), st["v_" + name]), name
+        assert not getattr(g, "grad_" + t).any()
+    assert int(rt.get_metadata().total_num_steps.item()) == 7
+
+
+def test_clustered_scene_with_bvh(oracle):
+    """A clustered scene large enough for a deep LBVH; oracle traverses its own (bit-identical) BVH."""
+    sc = synthetic.clustered_scene(60_000, seed=5)
+    rng = np.random.default_rng(1)
+    chan = rng.uniform(0, 1, (sc.n, 3)).astype(np.float32)
+    W, H = 96, 64
+    cam = synthetic.orbit_camera(0.4, W, H)
+    rt = G.make_tracer(W, H, sc.mean, sc.rotation, sc.scale, sc.opacity, channels=chan)
+    ro, rd = _camera_rays_gpu(rt, cam)
+    geom, l2w, aabb, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, sc.scale, sc.opacity)
+    tree = oracle.Bvh(aabb, vis)
+    fwd = oracle.trace_forward(ro, rd, geom, live, chan, vis, oracle.TraceConfig(), bvh=tree)
+    assert fwd["nhit"].sum() > W * H
+    _compare_forward(rt, fwd)

@@ -1,0 +1,153 @@
+"""Pins the CPU oracle to the reference (CPU only).
+
+Fixtures in tests/golden/ were made by tests/golden/make_golden.py from the reference's own test
+scenes (tests/test_single_gaussian.py, tests/test_multiple_gaussians.py) and from FP64
+restatements of its SH recurrence and Adam rule.
+"""
+import math
+
+import numpy as np
+import pytest
+
+FP16_ALPHA_BOUND = 2.0 ** -13 * 2.2  # half an fp16 ulp of alpha in [0.25, 0.5), times the colour sum bound
+
+
+def _scene(golden, name):
+    p = name + "_"
+    return {k: golden[p + k] for k in ("mean", "log_scale", "color", "rotation", "logit_opacity", "bg",
+                                       "alpha_threshold", "t_threshold")}
+
+
+def _run_oracle(O, golden, name, bvh=False):
+    s = _scene(golden, name)
+    a_thr = float(s["alpha_threshold"])
+    geom, l2w, aabb, vis = O.snapshot(s["mean"], s["rotation"], s["log_scale"], s["logit_opacity"][:, 0], a_thr)
+    live = O.forward_prep(s["logit_opacity"][:, 0], a_thr)
+    cfg = O.TraceConfig(alpha_threshold=a_thr, t_threshold=float(s["t_threshold"]), bg=tuple(s["bg"]))
+    tree = O.Bvh(aabb, vis) if bvh else None
+    out = O.trace_forward(golden["rays_o"], golden["rays_d"], geom, live, s["color"], vis, cfg, bvh=tree)
+    return s, cfg, geom, l2w, out
+
+
+NAMES = ["single_a0.01", "single_a0.3", "multi_t0.0", "multi_t0.5"]
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_image_matches_reference_rule(oracle, golden, name):
+    """Against the reference CUDA rule evaluated in FP64 (fp16 keys, 32-slot passes, tail
+    estimate): equal to float32 rounding except where an fp16 rounding midpoint separates the
+    FP64 and FP32 alpha (rare pixels, bounded by half an fp16 ulp of alpha)."""
+    s, cfg, *_ , out = _run_oracle(oracle, golden, name)
+    diff = np.abs(out["rgb"] - golden[name + "_rule64_rgb"]).max(axis=1)
+    assert np.mean(diff < 1e-6) >= 0.99
+    assert diff.max() < FP16_ALPHA_BOUND
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_image_matches_reference_tests(oracle, golden, name):
+    """Against the reference tests' FP64 loops: those composite with exact alpha, the reference
+    kernel with fp16 alpha; the difference is bounded by the fp16 quantisation of alpha."""
+    s, cfg, *_ , out = _run_oracle(oracle, golden, name)
+    ref = golden[name + "_ref64_rgb"]
+    err = np.abs(out["rgb"] - ref)
+    assert err.mean() < 1e-4
+    assert err.max() < 3e-4
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_gradients_match_reference_tests(oracle, golden, name):
+    """Gradients of the L1 loss against the reference tests' FP64 autograd, at the reference
+    tests' own tolerance (abs 1e-4, tests/test_single_gaussian.py:228-232)."""
+    s, cfg, geom, l2w, out = _run_oracle(oracle, golden, name)
+    grad = oracle.trace_backward(32, 32, golden["rays_o"], golden["rays_d"], out, golden[name + "_ref64_grad_out"],
+                                 geom, l2w, s["logit_opacity"], s["log_scale"], s["rotation"], s["color"], cfg)
+    pairs = [(slice(0, 4), "rotation"), (slice(4, 7), "mean"), (slice(7, 8), "logit_opacity"),
+             (slice(8, 11), "log_scale"), (slice(12, 15), "color")]
+    for sl, key in pairs:
+        ref = golden[name + "_ref64_grad_" + key]
+        assert np.abs(grad[:, sl] - ref).max() < 1e-4, key
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_bvh_traversal_equals_brute_force(oracle, golden, name):
+    *_, a = _run_oracle(oracle, golden, name)
+    *_, b = _run_oracle(oracle, golden, name, bvh=True)
+    assert np.array_equal(a["nhit"], b["nhit"])
+    assert np.array_equal(a["nacc"], b["nacc"])
+    assert np.array_equal(a["ids"], b["ids"])
+    assert np.array_equal(a["T"], b["T"])
+    assert np.array_equal(a["rem"], b["rem"])
+
+
+@pytest.mark.parametrize("deg", [0, 1, 2, 3])
+def test_oracle_sh_matches_reference_recurrence(oracle, golden_sh, deg):
+    g = golden_sh
+    col = oracle.sh_forward(deg, g["mean"], g["cam"], g["dc"][:, 0, :], g["rest"])
+    assert np.abs(col - g[f"deg{deg}_colour"]).max() < 5e-7
+    vis = np.ones(col.shape[0], np.uint8)
+    gdc, grest, gm = oracle.sh_backward(deg, g["mean"], g["cam"], g["rest"], col, g[f"deg{deg}_grad_colour"], vis,
+                                        np.zeros((col.shape[0], 3), np.float32))
+    assert np.abs(gdc - g[f"deg{deg}_grad_dc"][:, 0, :]).max() < 1e-6
+    assert np.abs(grest - g[f"deg{deg}_grad_rest"]).max() < 2e-6
+    assert np.abs(gm - g[f"deg{deg}_grad_mean"]).max() < 2e-6
+
+
+@pytest.mark.parametrize("step", [1, 7, 1000])
+def test_oracle_adam_matches_fp64_rule(oracle, golden_sh, step):
+    """cuda/opt/adam.cu:13-22 (bias-correction exponent step + 1) against its FP64 restatement."""
+    g = golden_sh
+    n = 16  # the 64 golden values ride in the rotation group ([16, 4])
+    st = {}
+    for name, width in (("channels", 3), ("opacity", 1), ("mean", 3), ("rotation", 4), ("scale", 3), ("sh_dc", 3),
+                        ("sh_rest", 0)):
+        for pre in ("", "g_", "m_", "v_"):
+            st[pre + name] = np.zeros(n * width, np.float32)
+    st["rotation"], st["m_rotation"], st["v_rotation"], st["g_rotation"] = (
+        g["adam_in_" + k].copy() for k in ("p", "m", "v", "g"))
+    oracle.adam_step(st, {"rotation": 0.01}, n, 0, step, zero_grads=True)
+    assert np.allclose(st["rotation"], g[f"adam_step{step}_p"], rtol=1e-6, atol=1e-7)
+    assert np.allclose(st["m_rotation"], g[f"adam_step{step}_m"], rtol=1e-6, atol=1e-9)
+    assert np.allclose(st["v_rotation"], g[f"adam_step{step}_v"], rtol=1e-6, atol=1e-12)
+    assert not st["g_rotation"].any()
+
+
+def _ulp_err(got, ref):
+    got = np.float32(got)
+    ref32 = np.float32(ref)
+    if not np.isfinite(ref32):
+        return 0 if got == ref32 else 99
+    return abs(float(got) - ref) / float(np.spacing(np.abs(ref32)))
+
+
+def test_own_exp_log_accuracy(oracle):
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([rng.uniform(-103, 88, 3000), rng.uniform(-1, 1, 2000), rng.uniform(-20, 0, 2000)])
+    worst = max(_ulp_err(oracle.expf(float(np.float32(x))), math.exp(float(np.float32(x)))) for x in xs)
+    assert worst <= 2.0
+    ys = np.concatenate([np.exp(rng.uniform(-80, 80, 3000)), rng.uniform(0.5, 2, 2000), rng.uniform(1e-3, 1e3, 2000)])
+    worst = max(_ulp_err(oracle.logf(float(np.float32(y))), math.log(float(np.float32(y)))) for y in ys)
+    assert worst <= 2.5
+    assert oracle.expf(0.0) == 1.0
+    assert oracle.logf(1.0) == 0.0
+
+
+def test_half_rounding_matches_ieee(oracle):
+    rng = np.random.default_rng(1)
+    v = np.concatenate([rng.uniform(0, 70000, 4000), np.exp(rng.uniform(-20, 11, 4000)), [0.0, 2.0 ** -25,
+                        2.0 ** -24, 65504.0, 65520.0, 1e-8]]).astype(np.float32)
+    lib = oracle.lib()
+    for x in v:
+        h = lib.orc_f2h(float(x))
+        assert h == int(np.float16(x).view(np.uint16)), x
+        assert lib.orc_h2f(h) == float(np.float16(x))
+
+
+def test_maxalpha_product_is_correctly_rounded(oracle):
+    rng = np.random.default_rng(2)
+    lib = oracle.lib()
+    bad = 0
+    for _ in range(5000):
+        a, b = np.float32(rng.uniform(0, 1)), np.float32(rng.uniform(0, 1))
+        ref = np.float32(0.9999 * float(a) * float(b))
+        bad += lib.orc_maxalpha_mul(float(a), float(b)) != ref
+    assert bad <= 2
