@@ -1,0 +1,381 @@
+#!/usr/bin/env python
+"""Benchmark: one training step of the Gaussian ray tracer at 3M Gaussians, 1920x1080.
+
+A step is what the reference's training loop does per image (train.py:245-287 minus the loss's
+SSIM term): SH colour + forward trace, L1 loss against a target image, reverse-replay backward +
+SH backward, fused Adam, BVH refit.  Synthetic, seeded inputs: 3M Gaussians drawn from 200
+anisotropic clusters inside a radius-10 sphere (log-scales N(-4.5, 0.5)), camera on a radius-8
+orbit, fx = fy = 1440, seeded random target image.  Inputs (3 GB of parameters and optimiser
+state) are far larger than L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line (rank 0).  `value` is train-steps/s with the target image resident in HBM;
+`e2e` is the same step through the public Raytracer API with the target copied from pinned host
+memory and the loss read back every step.  `roofline` is for the kernel with the largest share of
+the step, from CUDA events recorded around each launch inside the timed region.  `--impl
+reference` times the CPU restatement of the reference's algorithm (oracle/, the reference itself
+needs OptiX and does not build here) on a bounded sample of rays per step, extrapolated.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rays/s and train-steps/s at 3M Gaussians 1080p; served p50/p99 latency vs plain"
+LR = dict(mean=1.6e-4, scale=5e-3, rotation=1e-3, opacity=2.5e-2, sh=2.5e-3)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n-gaussians", type=int, default=3_000_000)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-stride", type=int, default=24, help="1 ray in stride^2 pixels for the CPU sample")
+    return ap.parse_args()
+
+
+def workload_config(a, rank=0):
+    return {"workload": f"train step, {a.n_gaussians / 1e6:g}M clustered Gaussians, {a.width}x{a.height}",
+            "n_gaussians": a.n_gaussians, "width": a.width, "height": a.height, "rays_per_step": a.width * a.height,
+            "sh_degree": 3, "t_threshold": 0.03, "alpha_threshold": 0.01, "exp_power": 2.0,
+            "l2": "inputs larger than L2 (no flush)", "seed": 0}
+
+
+def make_scene(a):
+    from gray_gb300 import synthetic
+
+    return synthetic.clustered_scene(a.n_gaussians, seed=0)
+
+
+def make_camera(a, rank):
+    from gray_gb300 import synthetic
+
+    return synthetic.orbit_camera(0.3 + 0.7 * rank, a.width, a.height)
+
+
+# ----------------------------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.gpu = gpu_index
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_gbs():
+    try:
+        m = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(m["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json"))).get(kernel)
+    except Exception:
+        return None
+
+
+def gpu_arm(a, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import torch.nn.functional as F
+
+    from gray_gb300 import RaytracerConfig, Raytracer, _lib
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    sc = make_scene(a)
+    cam = make_camera(a, rank)
+    cfg = RaytracerConfig(sh=True, sh_max_degree=3, lr_mean_init=LR["mean"], lr_scale_init=LR["scale"],
+                          lr_rotation_init=LR["rotation"], lr_opacity_init=LR["opacity"], lr_sh_dc_init=LR["sh"],
+                          lr_sh_rest=LR["sh"], ppll_backward_size=160_000_000)
+    rt = Raytracer(cfg, sc.n, a.width, a.height)
+    g = rt.cuda_module.get_gaussians()
+    with torch.no_grad():
+        g.mean.copy_(torch.from_numpy(sc.mean))
+        g.rotation.copy_(torch.from_numpy(sc.rotation))
+        g.scale.copy_(torch.from_numpy(sc.scale))
+        g.opacity.copy_(torch.from_numpy(sc.opacity))
+        g.sh_coeffs_dc.copy_(torch.from_numpy(sc.sh_dc))
+        g.sh_coeffs_rest.copy_(torch.from_numpy(sc.sh_rest))
+        g.current_sh_degree.fill_(3)
+    rt.cuda_module.rebuild_bvh()
+    gen = torch.Generator().manual_seed(1234 + rank)
+    target_host = torch.rand(3, a.height, a.width, generator=gen).pin_memory()
+    target_dev = target_host.to(dev)
+    loss_host = torch.zeros(1).pin_memory()
+    stream = torch.cuda.current_stream()
+
+    def train_step(target):
+        render = rt(cam)
+        loss = F.l1_loss(render, target)
+        rt.backward(loss)
+        rt.step()
+        return loss
+
+    def e2e_step():
+        target_dev.copy_(target_host, non_blocking=True)
+        loss = train_step(target_dev)
+        loss_host.copy_(loss.detach().reshape(1), non_blocking=True)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed(fn, k):
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    for _ in range(a.warmup):
+        train_step(target_dev)
+    torch.cuda.synchronize()
+    rt.cuda_module.check_status()
+
+    # ---- timed region: device-resident inputs ----
+    st = rt.cuda_module.get_stats()
+    st.reset()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    with _lib.Profiler(capacity=64 * (a.steps + 1)) as prof:
+        ms = timed(lambda: train_step(target_dev), a.steps)
+    clk = clocks.stop()
+    rt.cuda_module.check_status()
+    H = float(st.num_gaussians_hit.sum().item()) / a.steps
+    A = float(st.num_gaussians_accumulated.sum().item()) / a.steps
+    R = a.width * a.height
+    ms_step = ms / a.steps
+    steps_per_s = 1000.0 / ms_step * world
+
+    # ---- e2e through the public API with host buffers ----
+    for _ in range(max(1, a.warmup // 2)):
+        e2e_step()
+    ms_e2e = timed(e2e_step, a.steps)
+    e2e_steps_per_s = 1000.0 / (ms_e2e / a.steps) * world
+
+    # ---- render-only throughput (inference-style forward, no grads) ----
+    with torch.no_grad():
+        for _ in range(2):
+            rt(cam, skip_copy=True)
+        ms_render = timed(lambda: rt(cam, skip_copy=True), a.steps)
+    rays_per_s = R * a.steps / (ms_render / 1000.0) * world
+
+    # ---- roofline of the dominant kernel ----
+    res = prof.results
+    n = sc.n
+    algo = {
+        "trace_forward": 44.0 * H + 12.0 * A + 60.0 * R,
+        "trace_backward": 120.0 * A + 72.0 * R,
+        "forward_prep": 228.0 * n,
+        "fold_sh_backward": 460.0 * n,
+        "adam": 1984.0 * n,
+        "snapshot": (44.0 + 48 + 48 + 32) * n,
+        "refit": 44.0 * n + 24.0 * (2 * n - 1),
+    }
+    total_ms = sum(v[0] for v in res.values())
+    dominant = max(res, key=lambda k: res[k][0])
+    dom_ms = res[dominant][0] / res[dominant][1]
+    peak, peak_kind = measured_peak_gbs()
+    achieved = algo.get(dominant, 0.0) / (dom_ms / 1000.0) / 1e9
+    kernels_per_group = {"adam": 2}
+    launches = sum(cnt * kernels_per_group.get(name, 1) for name, (_, cnt) in res.items())
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "traffic": ncu_traffic(dominant), "algorithmic_bytes": algo.get(dominant),
+                "avg_launch_ms": round(dom_ms, 4),
+                "shares": {k: round(v[0] / total_ms, 4) for k, v in sorted(res.items(), key=lambda kv: -kv[1][0])},
+                "hits_per_ray": round(H / R, 2), "composited_per_ray": round(A / R, 2)}
+
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline:
+        cpu = cpu_baseline(a, sc, cam)
+
+    line = {"metric": METRIC, "value": round(steps_per_s, 3), "unit": "train-steps/s", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered scene)",
+            "config": dict(workload_config(a), parallelism=f"replicas x{world}"),
+            "rays_per_s": round(rays_per_s, 1), "train_rays_per_s": round(R * steps_per_s, 1),
+            "e2e": {"value": round(e2e_steps_per_s, 3), "unit": "train-steps/s",
+                    "h2d_bytes_per_step": int(target_host.numel() * 4), "d2h_bytes_per_step": 4},
+            "gpu_launches": launches, "roofline": roofline, "clocks": clk, "cpu_baseline": cpu}
+    return line
+
+
+# ----------------------------------------------------------------------------------------------
+# CPU restatement (oracle): baseline leg and reference arm
+# ----------------------------------------------------------------------------------------------
+class CpuScene:
+    """The oracle's view of the benchmark scene: snapshot, BVH, SH colours, sample rays."""
+
+    def __init__(self, a, sc, cam):
+        import numpy as np
+
+        from oracle import oracle as O
+
+        O.build()
+        self.O = O
+        self.a = a
+        self.threads = O.hardware_threads()
+        self.sc = sc
+        self.geom, self.l2w, self.aabb, self.vis = O.snapshot(sc.mean, sc.rotation, sc.scale, sc.opacity[:, 0])
+        self.live = O.forward_prep(sc.opacity[:, 0])
+        self.chan = O.sh_forward(3, sc.mean, cam.origin.astype(np.float32), sc.sh_dc[:, 0, :], sc.sh_rest)
+        self.bvh = O.Bvh(self.aabb, self.vis)
+        ro, rd = O.camera_rays(a.width, a.height, cam.fov_y, cam.origin.astype(np.float32), cam.rotation_c2w_blender())
+        s = a.cpu_sample_stride
+        ys, xs = np.meshgrid(np.arange(s // 2, a.height, s), np.arange(s // 2, a.width, s), indexing="ij")
+        idx = (ys * a.width + xs).ravel()
+        self.ro, self.rd = ro[idx], rd[idx]
+        self.cfg = O.TraceConfig(t_threshold=0.03)
+        self.rng = np.random.default_rng(0)
+
+    def step_seconds(self):
+        """One extrapolated CPU train step: trace forward + backward on the ray sample scaled to the
+        full image, plus SH, Adam, snapshot and refit over a slice of the Gaussians scaled to N."""
+        import numpy as np
+
+        O, a, sc = self.O, self.a, self.sc
+        R_full = a.width * a.height
+        t0 = time.perf_counter()
+        fwd = O.trace_forward(self.ro, self.rd, self.geom, self.live, self.chan, self.vis, self.cfg, bvh=self.bvh,
+                              nthreads=self.threads)
+        gout = np.sign(fwd["rgb"] - 0.5).astype(np.float32) / np.float32(3 * R_full)
+        O.trace_backward(a.width, a.height, self.ro, self.rd, fwd, gout, self.geom, self.l2w, sc.opacity, sc.scale,
+                         sc.rotation, self.chan, self.cfg, nthreads=self.threads)
+        t_trace = time.perf_counter() - t0
+        # per-Gaussian work on a slice (single thread), scaled to N
+        m = min(sc.n, 200_000)
+        t1 = time.perf_counter()
+        O.sh_forward(3, sc.mean[:m], np.zeros(3, np.float32), sc.sh_dc[:m, 0, :], sc.sh_rest[:m])
+        st = {}
+        for name, width in (("channels", 3), ("opacity", 1), ("mean", 3), ("rotation", 4), ("scale", 3),
+                            ("sh_dc", 3), ("sh_rest", 45)):
+            for pre in ("", "g_", "m_", "v_"):
+                st[pre + name] = np.zeros(m * width, np.float32)
+        O.adam_step(st, {"mean": 1e-4}, m, 15, 1)
+        g2, l2, aabb2, vis2 = O.snapshot(sc.mean[:m], sc.rotation[:m], sc.scale[:m], sc.opacity[:m, 0])
+        t_gauss = (time.perf_counter() - t1) * (sc.n / m)
+        return t_trace * (R_full / self.ro.shape[0]) + t_gauss, fwd
+
+
+def cpu_baseline(a, sc, cam):
+    cs = CpuScene(a, sc, cam)
+    t, fwd = cs.step_seconds()
+    return {"value": round(1.0 / t, 5), "unit": "train-steps/s", "cores": cs.threads, "kind": "port",
+            "sample": f"{cs.ro.shape[0]} rays (1 per {a.cpu_sample_stride}^2 pixels) traced forward+backward with the "
+                      f"oracle's BVH on {cs.threads} threads, scaled to {a.width}x{a.height}; SH/Adam/snapshot on "
+                      f"a 200k-Gaussian slice scaled to {a.n_gaussians}",
+            "hits_per_ray_sample": round(float(fwd["nhit"].mean()), 2)}
+
+
+def reference_arm(a, rank, world):
+    if rank != 0:
+        return None
+    sc = make_scene(a)
+    cam = make_camera(a, 0)
+    cs = CpuScene(a, sc, cam)
+    for _ in range(a.warmup):
+        cs.step_seconds()
+    times = [cs.step_seconds()[0] for _ in range(a.steps)]
+    t = sum(times) / len(times)
+    v = round(1.0 / t, 5)
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "train-steps/s", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1000 * t, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered scene)",
+            "config": dict(workload_config(a), parallelism="cpu"),
+            "cpu_baseline": {"value": v, "unit": "train-steps/s", "cores": cs.threads, "kind": "port",
+                             "sample": f"per step {cs.ro.shape[0]} rays forward+backward + 200k-Gaussian slice, "
+                                       "extrapolated to the full step; the reference (OptiX 8) does not build here"},
+            "e2e": {"value": v, "unit": "train-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    a = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and a.impl == "gb300":
+        import torch
+
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    if a.impl == "reference":
+        line = reference_arm(a, rank, world)
+    else:
+        line = gpu_arm(a, rank, world, local_rank)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1 and a.impl == "gb300":
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

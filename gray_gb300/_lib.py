@@ -76,7 +76,8 @@ class ParamsC(ctypes.Structure):
 
 
 ENTRY_POINTS = ("gray_forward_pass", "gray_forward_pass_display", "gray_backward_pass", "gray_step",
-                "gray_update_bvh", "gray_rebuild_bvh", "gray_sort_tmp_words", "gray_last_error", "gray_version")
+                "gray_update_bvh", "gray_rebuild_bvh", "gray_sort_tmp_words", "gray_profiler_enable",
+                "gray_profiler_collect", "gray_last_error", "gray_version")
 
 _lib = None
 
@@ -101,6 +102,10 @@ def load(path: str | None = None):
         f.argtypes = [ctypes.POINTER(ParamsC), ctypes.c_void_p]
     L.gray_sort_tmp_words.restype = ctypes.c_size_t
     L.gray_sort_tmp_words.argtypes = [ctypes.c_int32]
+    L.gray_profiler_enable.restype = ctypes.c_int
+    L.gray_profiler_enable.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.gray_profiler_collect.restype = ctypes.c_int
+    L.gray_profiler_collect.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.gray_last_error.restype = ctypes.c_char_p
     L.gray_version.restype = ctypes.c_char_p
     _lib = L
@@ -112,3 +117,35 @@ def call(name: str, params: ParamsC, stream: int):
     rc = getattr(L, name)(ctypes.byref(params), ctypes.c_void_p(stream))
     if rc != 0:
         raise GrayError(f"{name}: {L.gray_last_error().decode()} (code {rc})")
+
+
+class Profiler:
+    """Per-launch CUDA-event timing of the library's kernel groups (gray_profiler_* in the C ABI).
+
+        with Profiler() as prof:
+            ...                      # calls into the library
+        prof.results                 # {name: (total_ms, launches)}
+    """
+
+    def __init__(self, capacity: int = 8192):
+        self.capacity = capacity
+        self.results = {}
+
+    def __enter__(self):
+        L = load()
+        if L.gray_profiler_enable(1, self.capacity) != 0:
+            raise GrayError(L.gray_last_error().decode())
+        return self
+
+    def __exit__(self, *exc):
+        L = load()
+        L.gray_profiler_enable(0, 0)
+        buf = ctypes.create_string_buffer(1 << 16)
+        n = L.gray_profiler_collect(buf, len(buf))
+        if n < 0:
+            raise GrayError(L.gray_last_error().decode())
+        self.results = {}
+        for line in buf.value.decode().strip().splitlines():
+            name, ms, cnt = line.split()
+            self.results[name] = (float(ms), int(cnt))
+        return False

@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "gray_internal.h"
 
@@ -23,11 +24,6 @@ int cuda_fail(cudaError_t e, const char *where) {
     return GRAY_ERR_CUDA;
 }
 
-#define GRAY_TRY(expr, where)                                \
-    do {                                                     \
-        cudaError_t _e = (expr);                             \
-        if (_e != cudaSuccess) return cuda_fail(_e, where);  \
-    } while (0)
 
 bool frame_ok(const gray_params *p) {
     return p->render_width >= 1 && p->render_height >= 1 && p->render_width <= p->image_width &&
@@ -58,9 +54,94 @@ int check_trace(const gray_params *p) {
     return GRAY_OK;
 }
 
+// ---- optional per-launch timing (CUDA events on the launching stream) ----
+struct ProfRecord {
+    const char *name;
+    int ev;  // index of the start event; stop is ev + 1
+};
+bool g_prof_on = false;
+std::vector<cudaEvent_t> g_prof_events;
+std::vector<ProfRecord> g_prof_records;
+
+struct ProfScope {
+    bool on;
+    cudaStream_t s;
+    ProfScope(const char *name, cudaStream_t stream) : on(g_prof_on), s(stream) {
+        if (!on) return;
+        int ev = (int)g_prof_records.size() * 2;
+        if (ev + 1 >= (int)g_prof_events.size()) {
+            on = false;  // pool exhausted: stop recording rather than allocate in a timed region
+            return;
+        }
+        g_prof_records.push_back(ProfRecord{name, ev});
+        cudaEventRecord(g_prof_events[ev], s);
+    }
+    ~ProfScope() {
+        if (on) cudaEventRecord(g_prof_events[g_prof_records.back().ev + 1], s);
+    }
+};
+
 }  // namespace
 
+#define GRAY_LAUNCH(name, expr)                                      \
+    do {                                                             \
+        cudaError_t _e;                                              \
+        {                                                            \
+            ProfScope _ps(name, s);                                  \
+            _e = (expr);                                             \
+        }                                                            \
+        if (_e != cudaSuccess) return cuda_fail(_e, name);           \
+    } while (0)
+
 extern "C" {
+
+int gray_profiler_enable(int on, int capacity) {
+    if (on) {
+        if ((int)g_prof_events.size() < 2 * capacity) {
+            for (int i = (int)g_prof_events.size(); i < 2 * capacity; i++) {
+                cudaEvent_t e;
+                cudaError_t err = cudaEventCreate(&e);
+                if (err != cudaSuccess) return cuda_fail(err, "profiler event");
+                g_prof_events.push_back(e);
+            }
+        }
+        g_prof_records.clear();
+    }
+    g_prof_on = on != 0;
+    return GRAY_OK;
+}
+
+int gray_profiler_collect(char *buf, size_t buflen) {
+    // per launcher name: total milliseconds and launch count
+    std::vector<std::pair<std::string, std::pair<double, int>>> agg;
+    for (const ProfRecord &r : g_prof_records) {
+        cudaError_t err = cudaEventSynchronize(g_prof_events[r.ev + 1]);
+        if (err != cudaSuccess) return -cuda_fail(err, "profiler sync");
+        float ms = 0.0f;
+        err = cudaEventElapsedTime(&ms, g_prof_events[r.ev], g_prof_events[r.ev + 1]);
+        if (err != cudaSuccess) return -cuda_fail(err, "profiler elapsed");
+        bool found = false;
+        for (auto &a : agg)
+            if (a.first == r.name) {
+                a.second.first += ms;
+                a.second.second += 1;
+                found = true;
+            }
+        if (!found) agg.push_back({r.name, {ms, 1}});
+    }
+    std::string out;
+    for (auto &a : agg) {
+        char line[160];
+        snprintf(line, sizeof(line), "%s %.6f %d\n", a.first.c_str(), a.second.first, a.second.second);
+        out += line;
+    }
+    if (buf && buflen) {
+        strncpy(buf, out.c_str(), buflen - 1);
+        buf[buflen - 1] = 0;
+    }
+    g_prof_records.clear();
+    return (int)out.size();
+}
 
 size_t gray_sort_tmp_words(int32_t n) { return gray::sort_tmp_words(n); }
 
@@ -68,8 +149,8 @@ int gray_forward_pass(const gray_params *p, void *stream) {
     int e = check_trace(p);
     if (e) return e;
     cudaStream_t s = (cudaStream_t)stream;
-    GRAY_TRY(gray::launch_forward_prep(*p, true, s), "forward_prep");
-    GRAY_TRY(gray::launch_trace_forward(*p, s), "trace_forward");
+    GRAY_LAUNCH("forward_prep", gray::launch_forward_prep(*p, true, s));
+    GRAY_LAUNCH("trace_forward", gray::launch_trace_forward(*p, s));
     return GRAY_OK;
 }
 
@@ -77,8 +158,8 @@ int gray_forward_pass_display(const gray_params *p, void *stream) {
     int e = check_trace(p);
     if (e) return e;
     cudaStream_t s = (cudaStream_t)stream;
-    GRAY_TRY(gray::launch_forward_prep(*p, false, s), "forward_prep");
-    GRAY_TRY(gray::launch_trace_forward(*p, s), "trace_forward");
+    GRAY_LAUNCH("forward_prep", gray::launch_forward_prep(*p, false, s));
+    GRAY_LAUNCH("trace_forward", gray::launch_trace_forward(*p, s));
     return GRAY_OK;
 }
 
@@ -89,8 +170,8 @@ int gray_backward_pass(const gray_params *p, void *stream) {
     if (!p->scene.grad_acc || !p->gaussians.grad_mean)
         return fail(GRAY_ERR_INVALID_ARGUMENT, "missing gradient buffers");
     cudaStream_t s = (cudaStream_t)stream;
-    GRAY_TRY(gray::launch_trace_backward(*p, s), "trace_backward");
-    GRAY_TRY(gray::launch_fold_and_sh_backward(*p, s), "fold_sh_backward");
+    GRAY_LAUNCH("trace_backward", gray::launch_trace_backward(*p, s));
+    GRAY_LAUNCH("fold_sh_backward", gray::launch_fold_and_sh_backward(*p, s));
     return GRAY_OK;
 }
 
@@ -100,7 +181,8 @@ int gray_step(const gray_params *p, void *stream) {
     if (p->gaussians.sh_is_fp16) return fail(GRAY_ERR_INVALID_ARGUMENT, "step needs an inference_only=False raytracer");
     if (!p->gaussians.first_moment_mean || !p->metadata.total_num_steps)
         return fail(GRAY_ERR_INVALID_ARGUMENT, "missing optimiser state");
-    GRAY_TRY(gray::launch_adam(*p, (cudaStream_t)stream), "adam");
+    cudaStream_t s = (cudaStream_t)stream;
+    GRAY_LAUNCH("adam", gray::launch_adam(*p, s));
     return GRAY_OK;
 }
 
@@ -110,8 +192,8 @@ int gray_update_bvh(const gray_params *p, void *stream) {
     if (p->gaussians.count > 0 && !p->scene.bvh_valid)
         return fail(GRAY_ERR_INVALID_ARGUMENT, "update_bvh before rebuild_bvh");
     cudaStream_t s = (cudaStream_t)stream;
-    GRAY_TRY(gray::launch_snapshot(*p, s), "snapshot");
-    GRAY_TRY(gray::launch_lbvh_refit(*p, s), "refit");
+    GRAY_LAUNCH("snapshot", gray::launch_snapshot(*p, s));
+    GRAY_LAUNCH("refit", gray::launch_lbvh_refit(*p, s));
     return GRAY_OK;
 }
 
@@ -121,8 +203,8 @@ int gray_rebuild_bvh(const gray_params *p, void *stream) {
     if (!p->scene.geom || !p->scene.nodes || !p->scene.sort_tmp)
         return fail(GRAY_ERR_INVALID_ARGUMENT, "missing scene workspace");
     cudaStream_t s = (cudaStream_t)stream;
-    GRAY_TRY(gray::launch_snapshot(*p, s), "snapshot");
-    GRAY_TRY(gray::launch_lbvh_build(*p, s), "lbvh_build");
+    GRAY_LAUNCH("snapshot", gray::launch_snapshot(*p, s));
+    GRAY_LAUNCH("lbvh_build", gray::launch_lbvh_build(*p, s));
     return GRAY_OK;
 }
 

@@ -185,6 +185,16 @@ int gray_update_bvh(const gray_params *p, void *stream);
  * and full LBVH build (Morton codes, radix sort, Karras hierarchy, bottom-up boxes). */
 int gray_rebuild_bvh(const gray_params *p, void *stream);
 
+/* Optional timing of every launch made by the entry points above, with CUDA events recorded
+ * on the caller's stream around each kernel group (forward_prep, trace_forward, trace_backward,
+ * fold_sh_backward, adam, snapshot, refit, lbvh_build).  No reference counterpart: profiling
+ * support for the benchmark harness.  enable(1, capacity) pre-creates 2*capacity events and
+ * clears the records; enable(0, 0) stops recording.  collect() waits for the recorded events,
+ * writes "name total_ms launches\n" lines into buf and clears the records; it returns the
+ * length of the full text, or minus a GRAY_ERR_* code.  Not thread-safe; not for use inside stream capture. */
+int gray_profiler_enable(int on, int capacity);
+int gray_profiler_collect(char *buf, size_t buflen);
+
 /* Message of the last error returned on the calling thread. */
 const char *gray_last_error(void);
 

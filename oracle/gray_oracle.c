@@ -866,14 +866,43 @@ void orc_trace_forward(int nrays, const float *ray_o, const float *ray_d, int n,
 /* ------------------------------------------------------------------------------------------ */
 /* trace backward: cuda/backward_pass.cu:2-142                                                 */
 /* ------------------------------------------------------------------------------------------ */
-void orc_trace_backward(int nrays, int launch_w, int launch_h, const float *ray_o, const float *ray_d,
-                        const float *pix_T, const float *pix_fullT, const float *pix_rem, const float *grad_out,
-                        const int64_t *comp_offsets, const uint32_t *comp_ids, int n, const float *geom,
-                        const float *l2w, const float *opacity, const float *scale, const float *rotation,
-                        const float *channels, const orc_trace_cfg *cfg, float eps_scale_grad, double *grad) {
-    (void)n;
+static inline void atomic_add_double(double *addr, double v) {
+    uint64_t old_bits, new_bits;
+    double old_v, new_v;
+    __atomic_load(addr, &old_v, __ATOMIC_RELAXED);
+    do {
+        new_v = old_v + v;
+        memcpy(&old_bits, &old_v, 8);
+        memcpy(&new_bits, &new_v, 8);
+    } while (!__atomic_compare_exchange((uint64_t *)addr, &old_bits, &new_bits, 0, __ATOMIC_RELAXED,
+                                        __ATOMIC_RELAXED) &&
+             (memcpy(&old_v, &old_bits, 8), 1));
+}
+
+typedef struct {
+    int r0, r1, launch_w, launch_h;
+    const float *ray_o, *ray_d, *pix_T, *pix_fullT, *pix_rem, *grad_out;
+    const int64_t *comp_offsets;
+    const uint32_t *comp_ids;
+    const float *geom, *l2w, *opacity, *scale, *rotation, *channels;
+    const orc_trace_cfg *cfg;
+    float eps_scale_grad;
+    double *grad;
+    int atomic;
+} bwd_job;
+
+static void backward_range(const bwd_job *J) {
+    const int launch_w = J->launch_w, launch_h = J->launch_h;
+    const float *ray_o = J->ray_o, *ray_d = J->ray_d, *pix_T = J->pix_T, *pix_fullT = J->pix_fullT;
+    const float *pix_rem = J->pix_rem, *grad_out = J->grad_out, *geom = J->geom, *l2w = J->l2w;
+    const float *opacity = J->opacity, *scale = J->scale, *rotation = J->rotation, *channels = J->channels;
+    const int64_t *comp_offsets = J->comp_offsets;
+    const uint32_t *comp_ids = J->comp_ids;
+    const orc_trace_cfg *cfg = J->cfg;
+    const float eps_scale_grad = J->eps_scale_grad;
+    double *grad = J->grad;
     const float npix = (float)(launch_w * launch_h);
-    for (int r = 0; r < nrays; r++) {
+    for (int r = J->r0; r < J->r1; r++) {
         const float *ro = ray_o + 3 * (size_t)r, *rd = ray_d + 3 * (size_t)r;
         const float *gout = grad_out + 3 * (size_t)r;
         const float *rem = pix_rem + 3 * (size_t)r;
@@ -957,16 +986,54 @@ void orc_trace_backward(int nrays, int launch_w, int launch_h, const float *ray_
             float dq = gq[0] * qr[0] + gq[1] * qr[1] + gq[2] * qr[2] + gq[3] * qr[3];
             float l3 = qlen * qlen * qlen;
             double *G = grad + 16 * (size_t)gid;
-            for (int k = 0; k < 4; k++) G[k] += (double)(dq * -qr[k] / l3 + gq[k] / qlen);
-            for (int k = 0; k < 3; k++) G[4 + k] += (double)(-gxw[k]);
-            G[7] += (double)go;
-            for (int k = 0; k < 3; k++) G[8 + k] += (double)gs[k];
-            G[11] += (double)(w / npix);
-            for (int k = 0; k < 3; k++) G[12 + k] += (double)(gout[k] * w);
-            G[15] += 1.0;
+            double v[16];
+            for (int k = 0; k < 4; k++) v[k] = (double)(dq * -qr[k] / l3 + gq[k] / qlen);
+            for (int k = 0; k < 3; k++) v[4 + k] = (double)(-gxw[k]);
+            v[7] = (double)go;
+            for (int k = 0; k < 3; k++) v[8 + k] = (double)gs[k];
+            v[11] = (double)(w / npix);
+            for (int k = 0; k < 3; k++) v[12 + k] = (double)(gout[k] * w);
+            v[15] = 1.0;
+            if (J->atomic)
+                for (int k = 0; k < 16; k++) atomic_add_double(G + k, v[k]);
+            else
+                for (int k = 0; k < 16; k++) G[k] += v[k];
             T = T / om;
         }
     }
+}
+
+static void *bwd_worker(void *arg) {
+    backward_range((const bwd_job *)arg);
+    return NULL;
+}
+
+void orc_trace_backward(int nrays, int launch_w, int launch_h, const float *ray_o, const float *ray_d,
+                        const float *pix_T, const float *pix_fullT, const float *pix_rem, const float *grad_out,
+                        const int64_t *comp_offsets, const uint32_t *comp_ids, int n, const float *geom,
+                        const float *l2w, const float *opacity, const float *scale, const float *rotation,
+                        const float *channels, const orc_trace_cfg *cfg, float eps_scale_grad, double *grad,
+                        int nthreads) {
+    (void)n;
+    if (nthreads <= 0) nthreads = orc_hardware_threads();
+    if (nthreads > nrays) nthreads = nrays > 0 ? nrays : 1;
+    bwd_job base = {0, nrays, launch_w, launch_h, ray_o, ray_d, pix_T, pix_fullT, pix_rem, grad_out, comp_offsets,
+                    comp_ids, geom, l2w, opacity, scale, rotation, channels, cfg, eps_scale_grad, grad, nthreads > 1};
+    if (nthreads == 1) {
+        backward_range(&base);
+        return;
+    }
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    bwd_job *jobs = (bwd_job *)malloc(sizeof(bwd_job) * (size_t)nthreads);
+    for (int t = 0; t < nthreads; t++) {
+        jobs[t] = base;
+        jobs[t].r0 = (int)((long long)nrays * t / nthreads);
+        jobs[t].r1 = (int)((long long)nrays * (t + 1) / nthreads);
+        pthread_create(&th[t], NULL, bwd_worker, &jobs[t]);
+    }
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    free(th);
+    free(jobs);
 }
 
 /* ------------------------------------------------------------------------------------------ */

@@ -104,7 +104,8 @@ void orc_trace_backward(int nrays, int launch_w, int launch_h, const float *ray_
                         const float *pix_T, const float *pix_fullT, const float *pix_rem, const float *grad_out,
                         const int64_t *comp_offsets, const uint32_t *comp_ids, int n, const float *geom,
                         const float *l2w, const float *opacity, const float *scale, const float *rotation,
-                        const float *channels, const orc_trace_cfg *cfg, float eps_scale_grad, double *grad);
+                        const float *channels, const orc_trace_cfg *cfg, float eps_scale_grad, double *grad,
+                        int nthreads);
 
 /* ---- fused Adam (cuda/opt/adam.cu:6-83) ----
  * arrays follow the reference holders; step = total_num_steps after the increment. */

@@ -93,7 +93,8 @@ def lib():
             ctypes.c_void_p, ctypes.c_int]
         L.orc_trace_backward.argtypes = [
             ctypes.c_int, ctypes.c_int, ctypes.c_int, F32P, F32P, F32P, F32P, F32P, F32P, I64P, U32P,
-            ctypes.c_int, F32P, F32P, F32P, F32P, F32P, F32P, ctypes.POINTER(_TraceCfg), ctypes.c_float, F64P]
+            ctypes.c_int, F32P, F32P, F32P, F32P, F32P, F32P, ctypes.POINTER(_TraceCfg), ctypes.c_float, F64P,
+            ctypes.c_int]
         L.orc_hardware_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -256,7 +257,7 @@ def trace_forward(ray_o, ray_d, geom, live, channels, visible, cfg: TraceConfig,
 
 
 def trace_backward(launch_w, launch_h, ray_o, ray_d, fwd, grad_out, geom, l2w, opacity, scale, rotation, channels,
-                   cfg: TraceConfig, eps_scale_grad=1e-12):
+                   cfg: TraceConfig, eps_scale_grad=1e-12, nthreads=1):
     """Per-Gaussian gradient accumulators (double) laid out as
     (rot4 | mean3, opacity | scale3, pruning | channels3, count)."""
     n = geom.shape[0]
@@ -268,7 +269,7 @@ def trace_backward(launch_w, launch_h, ray_o, ray_d, fwd, grad_out, geom, l2w, o
         ray_o.shape[0], launch_w, launch_h, _f32(ray_o), _f32(ray_d), _f32(fwd["T"]), _f32(fwd["fullT"]),
         _f32(fwd["rem"]), _f32(grad_out), np.ascontiguousarray(fwd["offsets"], dtype=np.int64), ids, n, _f32(geom),
         _f32(l2w), _f32(opacity).reshape(-1), _f32(scale), _f32(rotation), _f32(channels), ctypes.byref(cfg.c()),
-        eps_scale_grad, grad)
+        eps_scale_grad, grad, nthreads)
     return grad
 
 

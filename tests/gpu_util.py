@@ -22,6 +22,8 @@ def make_tracer(width, height, mean, rotation, scale, opacity, channels=None, sh
     cfg.render_depth.fill_(render_depth)
     cfg.enable_sh.fill_(sh_dc is not None)
     cfg.zero_grads.fill_(False)
+    rt.get_camera().znear.fill_(0.0)
+    rt.get_camera().zfar.fill_(99999.9)
     g = rt.get_gaussians()
     with torch.no_grad():
         g.mean.copy_(torch.from_numpy(np.asarray(mean, np.float32)))

@@ -37,10 +37,15 @@ def _compare_forward(rt, fwd, check_lists=True):
     nhit = st.num_gaussians_hit.reshape(-1).cpu().numpy()
     nacc = st.num_gaussians_accumulated.reshape(-1).cpu().numpy()
     alive = fwd["nhit"] >= 0
-    assert np.array_equal(nhit[alive], fwd["nhit"][alive])
-    assert np.array_equal(nacc[alive], fwd["nacc"][alive])
-    assert np.array_equal(f["transmittance"][alive, 0], fwd["T"][alive])
-    assert np.array_equal(f["remaining_channels_estimate"][alive], fwd["rem"][alive])
+
+    def same(name, a, b):
+        bad = np.nonzero(np.any((a != b).reshape(a.shape[0], -1), axis=1))[0]
+        assert bad.size == 0, f"{name}: {bad.size} rays differ, first {bad[:5]}: gpu {a[bad[:3]]} oracle {b[bad[:3]]}"
+
+    same("nhit", nhit[alive], fwd["nhit"][alive])
+    same("nacc", nacc[alive], fwd["nacc"][alive])
+    same("T", f["transmittance"][alive, 0], fwd["T"][alive])
+    same("rem", f["remaining_channels_estimate"][alive], fwd["rem"][alive])
     assert np.allclose(f["full_transmittance"][alive, 0], fwd["fullT"][alive], rtol=2e-6, atol=1e-7)
     assert np.abs(f["output_channels"][alive] - fwd["rgb"][alive]).max() < RGB_TOL
     if check_lists:
