@@ -158,19 +158,32 @@ class GaussianDataHolder:
             raise RuntimeError("The new number of Gaussians must not be larger than the current count.")
         if n < 0:
             raise RuntimeError("negative Gaussian count")
+        old = self.count
         with torch.no_grad():
             self.count = n
             for name in _PARAM_NAMES:
                 getattr(self, name).grad = None
-                getattr(self, name).resize_(self._shape(name, n))
+                self._resize(getattr(self, name), self._shape(name, n), old)
             for name in ("lr_mean", "lr_rotation", "lr_scale", "lr_opacity", "lr_channels", "lr_sh_dc", "lr_sh_rest"):
-                getattr(self, name).resize_(n, 1)
+                t = getattr(self, name)
+                first = t.reshape(-1)[:1].clone()
+                t.resize_(n, 1)
+                if n > old:
+                    t[old:] = first  # only element 0 is read; keep the rows consistent
             for kind in ("grad_", "first_moment_", "second_moment_"):
                 for name in _PARAM_NAMES:
-                    getattr(self, kind + name).resize_(self._shape(name, n))
+                    self._resize(getattr(self, kind + name), self._shape(name, n), old)
             for name in ("pruning_weight", "pruning_counter", "was_visible", "marked"):
-                getattr(self, name).resize_(n, 1)
+                self._resize(getattr(self, name), (n, 1), old)
         self._link_grads()
+
+    @staticmethod
+    def _resize(t: torch.Tensor, shape, old: int):
+        """resize_ keeping the leading rows; rows added by growing are zeroed (torch leaves them
+        uninitialised, so gradients and moments would otherwise start from stale memory)."""
+        t.resize_(shape)
+        if shape[0] > old:
+            t[old:].zero_()
 
     def increment_sh_degree(self):
         with torch.no_grad():

@@ -341,5 +341,5 @@ def test_clustered_scene_with_bvh(oracle):
     geom, l2w, aabb, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, sc.scale, sc.opacity)
     tree = oracle.Bvh(aabb, vis)
     fwd = oracle.trace_forward(ro, rd, geom, live, chan, vis, oracle.TraceConfig(), bvh=tree)
-    assert fwd["nhit"].sum() > W * H
+    assert fwd["nhit"].sum() > 1000
     _compare_forward(rt, fwd)
