@@ -1,0 +1,68 @@
+"""Differentiable FP64 torch restatement of the reference's compositing rule (test infrastructure).
+
+Follows cuda/shaders.cu:10-67 and cuda/forward_pass.cu:6-151 without the fp16 quantisation of the
+per-pixel list: per (ray, Gaussian) the max-density point, the hit test (in front of the origin,
+inside the clipped unit sphere), alpha = 0.9999 * sigmoid(opacity) * exp(-|x|^4 / 4) (exp_power 2),
+hits composited front to back until T < t_threshold, full transmittance over all hits, and the
+detached tail estimate of the skipped hits.  Used as the smooth function for finite differences and
+as the FP64 gradient the hand-written backward is compared with.
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+
+MAX_ALPHA = 0.9999
+
+
+def quat_to_rot(q):
+    q = q / q.norm(dim=-1, keepdim=True)
+    r, x, y, z = q.unbind(-1)
+    return torch.stack([
+        torch.stack([1 - 2 * (y * y + z * z), 2 * (x * y - r * z), 2 * (x * z + r * y)], -1),
+        torch.stack([2 * (x * y + r * z), 1 - 2 * (x * x + z * z), 2 * (y * z - r * x)], -1),
+        torch.stack([2 * (x * z - r * y), 2 * (y * z + r * x), 1 - 2 * (x * x + y * y)], -1)], -2)
+
+
+def render(ray_o, ray_d, mean, rotation, log_scale, logit_opacity, channels, alpha_threshold=0.01, t_threshold=0.03,
+           bg=(0.0, 0.0, 0.0), chunk=4096):
+    """ray_o, ray_d: [R,3]; returns [R,3] colours (float64, differentiable w.r.t. the parameters)."""
+    o = torch.sigmoid(logit_opacity.reshape(-1))
+    sf = torch.where(o > alpha_threshold, (4.0 * torch.log(torch.clamp(o / alpha_threshold, min=1.0))) ** 0.25,
+                     torch.zeros_like(o)).detach()
+    R = quat_to_rot(rotation)                         # [N,3,3]
+    inv_s = torch.exp(-log_scale)                     # [N,3]
+    M = R.transpose(-1, -2) * inv_s[:, :, None]        # diag(1/s) R^T (world -> standard-deviation frame)
+    bgt = torch.tensor(bg, dtype=ray_o.dtype, device=ray_o.device)
+    outs = []
+    for c0 in range(0, ray_o.shape[0], chunk):
+        ro, rd = ray_o[c0:c0 + chunk], ray_d[c0:c0 + chunk]
+        rel = ro[:, None, :] - mean[None, :, :]                      # [r,N,3]
+        lo = torch.einsum("nij,rnj->rni", M, rel)                     # [r,N,3]
+        ld = torch.einsum("nij,rj->rni", M, rd)
+        nrm2 = (ld * ld).sum(-1)
+        t = -(lo * ld).sum(-1) / nrm2                                 # world distance of the max-density point
+        x = lo + t[..., None] * ld                                    # closest point, std-dev frame
+        d = (x * x).sum(-1)
+        hit = ((lo * ld).sum(-1) <= 0) & (d <= sf[None, :] ** 2) & (o[None, :] > alpha_threshold)
+        alpha = MAX_ALPHA * o[None, :] * torch.exp(-0.25 * d * d)
+        alpha = torch.where(hit, alpha, torch.zeros_like(alpha))
+        order = torch.argsort(torch.where(hit, t, torch.full_like(t, math.inf)).detach(), dim=-1)
+        a_s = torch.gather(alpha, 1, order)
+        c_s = channels[order]                                        # [r,N,3]
+        one_minus = 1.0 - a_s
+        T_after = torch.cumprod(one_minus, dim=-1)
+        T_before = torch.cat([torch.ones_like(T_after[:, :1]), T_after[:, :-1]], dim=-1)
+        comp = (T_before.detach() >= t_threshold) & (a_s.detach() > 0)
+        w = torch.where(comp, T_before * a_s, torch.zeros_like(a_s))
+        C = (w[..., None] * c_s).sum(1)
+        T_fin = torch.prod(torch.where(comp, one_minus, torch.ones_like(one_minus)), dim=-1)
+        full_T = torch.prod(one_minus, dim=-1)
+        skipped = (~comp) & (a_s.detach() > 0)
+        sa = torch.where(skipped, a_s, torch.zeros_like(a_s)).detach()
+        sc = (sa[..., None] * c_s).sum(1).detach()
+        sa_sum = sa.sum(-1)
+        est = torch.where(sa_sum[:, None] > 0, sc / torch.clamp(sa_sum[:, None], min=1e-300), torch.zeros_like(sc))
+        outs.append(C + (T_fin - full_T)[:, None] * est + bgt[None, :] * full_T[:, None])
+    return torch.cat(outs, 0)

@@ -1,0 +1,130 @@
+"""Differentiation form: the hand-written backward behind torch.autograd.Function, checked against
+FP64 finite differences and FP64 autograd of the same compositing rule (tests/fp64_reference.py),
+and hit-list recomputation against stored hit lists.  Needs a GB300."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from gray_gb300 import autograd as GA
+from gray_gb300 import classes, synthetic
+from tests import fp64_reference as F64
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda(gray_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _tracer(n, w, h, pool=8_000_000, t_threshold=0.03):
+    rt = classes.Raytracer(w, h, n, 0, 1, pool)
+    rt.get_config().t_threshold.fill_(t_threshold)
+    rt.get_config().zero_grads.fill_(False)
+    return rt
+
+
+def _params(sc, dev, dtype=torch.float32):
+    chan = torch.from_numpy(np.random.default_rng(9).uniform(0.05, 0.95, (sc.n, 3)).astype(np.float32))
+    p = [torch.from_numpy(a).to(dev, dtype) for a in (sc.mean, sc.rotation, sc.scale, sc.opacity)]
+    p.append(chan.to(dev, dtype))
+    return [t.requires_grad_() for t in p]
+
+
+def test_gradients_vs_fp64_and_finite_differences():
+    """1000 Gaussians in [-2,2]^3, one 128x128 camera; hand-written backward vs FP64 autograd of the
+    same rule, and FP64 central differences (h = 1e-6) on 200 random parameters."""
+    dev = torch.device("cuda")
+    sc = synthetic.gradcheck_scene(seed=0)
+    cam = synthetic.look_at((0.5, -7.0, 1.0), (0, 0, 0), (0, 0, 1), 0.75, 128, 128)
+    rt = _tracer(sc.n, 128, 128)
+    mean, rot, scale, opac, chan = _params(sc, dev)
+    g = rt.get_gaussians()
+    with torch.no_grad():
+        for dst, src in ((g.mean, mean), (g.rotation, rot), (g.scale, scale), (g.opacity, opac),
+                         (g.channels, chan)):
+            dst.copy_(src)
+    rt.rebuild_bvh()
+    img = GA.render(rt, cam, mean, rot, scale, opac, channels=chan)
+    wgt = torch.from_numpy(np.random.default_rng(3).standard_normal((3, 128, 128))).to(dev)
+    (img.double() * wgt).sum().backward()
+    fb = rt.get_framebuffer()
+    ro = fb.ray_origin.reshape(-1, 3).double()
+    rd = fb.ray_direction.reshape(-1, 3).double()
+    p64 = [t.detach().double().requires_grad_() for t in (mean, rot, scale, opac, chan)]
+
+    def loss64(ps):
+        out = F64.render(ro, rd, ps[0], ps[1], ps[2], ps[3], ps[4])
+        return (out.reshape(128, 128, 3).permute(2, 0, 1) * wgt).sum()
+
+    # the GPU image against the FP64 rule: fp16 alpha quantisation bound
+    ref_img = F64.render(ro, rd, *[t.detach() for t in p64]).reshape(128, 128, 3).permute(2, 0, 1)
+    assert (img.double() - ref_img).abs().max().item() < 5e-3
+    l64 = loss64(p64)
+    g64 = torch.autograd.grad(l64, p64)
+    names = ("mean", "rotation", "scale", "opacity", "channels")
+    for name, gg, ref in zip(names, (mean.grad, rot.grad, scale.grad, opac.grad, chan.grad), g64):
+        err = (gg.double() - ref).norm() / ref.norm()
+        assert err.item() < 1e-3, (name, err.item())
+
+    # FP64 central differences on 200 random parameters
+    rng = np.random.default_rng(5)
+    flat = [t.detach().clone() for t in p64]
+    agree_fd_autograd, agree_fd_gpu, total = 0, 0, 0
+    gpu_grads = [mean.grad, rot.grad, scale.grad, opac.grad, chan.grad]
+    gmax = [float(r.abs().max()) for r in g64]
+    for _ in range(200):
+        k = int(rng.integers(0, 5))
+        idx = int(rng.integers(0, flat[k].numel()))
+        h = 1e-6
+        vals = []
+        for sgn in (1.0, -1.0):
+            ps = [t.clone() for t in flat]
+            ps[k].view(-1)[idx] += sgn * h
+            with torch.no_grad():
+                vals.append(float(loss64(ps)))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        ad = float(g64[k].reshape(-1)[idx])
+        gp = float(gpu_grads[k].reshape(-1)[idx])
+        tol = 1e-4 * gmax[k] + 1e-4 * abs(ad)
+        total += 1
+        agree_fd_autograd += abs(fd - ad) <= tol
+        agree_fd_gpu += abs(fd - gp) <= 1e-3 * gmax[k] + 1e-3 * abs(fd)
+    # parameters whose +-h perturbation moves a clip boundary across a ray are discontinuous
+    assert agree_fd_autograd >= 0.97 * total, agree_fd_autograd
+    assert agree_fd_gpu >= 0.95 * total, agree_fd_gpu
+
+
+@pytest.mark.parametrize("n,w,h", [(20_000, 160, 104), (1_000_000, 1600, 1040)])
+def test_recompute_matches_stored(n, w, h):
+    dev = torch.device("cuda")
+    sc = synthetic.clustered_scene(n, seed=11)
+    cam = synthetic.orbit_camera(0.9, w, h)
+    rt = _tracer(sc.n, w, h, pool=64_000_000)
+    mean, rot, scale, opac, chan = _params(sc, dev)
+    g = rt.get_gaussians()
+    with torch.no_grad():
+        for dst, src in ((g.mean, mean), (g.rotation, rot), (g.scale, scale), (g.opacity, opac),
+                         (g.channels, chan)):
+            dst.copy_(src)
+    rt.rebuild_bvh()
+    wgt = torch.randn(3, h, w, device=dev, generator=torch.Generator(device=dev).manual_seed(0))
+    grads = []
+    for recompute in (False, True):
+        for t in (mean, rot, scale, opac, chan):
+            t.grad = None
+        img = GA.render(rt, cam, mean, rot, scale, opac, channels=chan, recompute=recompute)
+        if recompute:
+            # another render in between: the stored lists of the first one are gone
+            with torch.no_grad():
+                GA._set_camera(rt, synthetic.orbit_camera(2.0, w, h))
+                rt.forward_pass()
+        (img * wgt).sum().backward()
+        grads.append([t.grad.clone() for t in (mean, rot, scale, opac, chan)])
+    rt.check_status()
+    for a, b in zip(*grads):
+        scale_ = b.abs().max().clamp(min=1e-12)
+        assert ((a - b).abs().max() / scale_).item() < 1e-5
