@@ -83,6 +83,10 @@ struct ProfScope {
 
 }  // namespace
 
+namespace gray {
+void set_last_error(const char *what) { g_last_error = what; }
+}  // namespace gray
+
 #define GRAY_LAUNCH(name, expr)                                      \
     do {                                                             \
         cudaError_t _e;                                              \

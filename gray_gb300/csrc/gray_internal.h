@@ -26,6 +26,9 @@ cudaError_t launch_trace_backward(const gray_params &p, cudaStream_t s);
 // adam.cu
 cudaError_t launch_adam(const gray_params &p, cudaStream_t s);
 
+// capi.cu: message returned by gray_last_error() on this thread
+void set_last_error(const char *what);
+
 constexpr int kThreads = 256;
 inline unsigned int blocks_for(long long n, int threads = kThreads) {
     return (unsigned int)((n + threads - 1) / threads);

@@ -195,6 +195,21 @@ int gray_rebuild_bvh(const gray_params *p, void *stream);
 int gray_profiler_enable(int on, int capacity);
 int gray_profiler_collect(char *buf, size_t buflen);
 
+/* Raytracer::rebuild_bvh without caller-provided scratch.  No counterpart in the reference: an
+ * addition for callers that cannot allocate device memory (a host that owns the whole device
+ * budget, such as an engine or viewer plugin, or a point in its code where its allocator must
+ * not be entered).  Same outputs as gray_rebuild_bvh (snapshot records, nodes, parents, order,
+ * codes, root box, all in p->scene); p->scene.sort_tmp, .bounds and .refit_flags are ignored
+ * and may be NULL.  The scratch is a fixed device array inside the library, sized for at most
+ * GRAY_STATIC_MAX_GAUSSIANS Gaussians (about 3.3 MB, held by every device that loads the
+ * library until the process exits); larger counts return GRAY_ERR_OUT_OF_RANGE.  The first call
+ * on each device looks up that array's device address (cudaGetSymbolAddress, with the device
+ * current), so make the first call before any stream capture.  Every call shares the one array:
+ * calls whose work overlaps on the GPU (other streams, other threads) race and must be
+ * serialised by the caller.  No allocation of any kind is made. */
+#define GRAY_STATIC_MAX_GAUSSIANS 262144
+int gray_rebuild_bvh_static(const gray_params *p, void *stream);
+
 /* Message of the last error returned on the calling thread. */
 const char *gray_last_error(void);
 
