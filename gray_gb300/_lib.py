@@ -72,7 +72,7 @@ class ParamsC(ctypes.Structure):
                 ("render_width", ctypes.c_uint32), ("render_height", ctypes.c_uint32),
                 ("camera", CameraC), ("config", ConfigC), ("framebuffer", FramebufferC), ("gaussians", GaussiansC),
                 ("metadata", MetadataC), ("stats", StatsC), ("hitlist", HitlistC), ("scene", SceneC),
-                ("status", P)]
+                ("status", P), ("trace_variant", ctypes.c_int32)]
 
 
 ENTRY_POINTS = ("gray_forward_pass", "gray_forward_pass_display", "gray_backward_pass", "gray_step",

@@ -325,6 +325,7 @@ class Raytracer:
         self.ppll_backward_data = PPLLDataHolder("backward", self.width, self.height,
                                                  1 if inference_only else ppll_backward_size, dev)
         self.status = torch.zeros(1, device=dev, dtype=torch.int32)
+        self.trace_variant = 0  # forward-kernel variant (0 = library default); results do not depend on it
         self._scene = _SceneWorkspace(1, dev)
         self._params = None
         if num_gaussians > 0:
@@ -359,6 +360,7 @@ class Raytracer:
         p.hitlist.size = h.size
         p.scene = self._scene.struct()
         p.status = _p(self.status)
+        p.trace_variant = int(self.trace_variant)
         return p
 
     def _call(self, name: str):
@@ -399,6 +401,12 @@ class Raytracer:
     def resize(self, new_num_gaussians: int):
         self.gaussian_data.resize(new_num_gaussians)
         self._scene = _SceneWorkspace(self.gaussian_data.count, self.device)
+        self._invalidate()
+
+    def set_trace_variant(self, variant: int):
+        """Select the forward-trace kernel variant (0 = default); every variant gives identical
+        results."""
+        self.trace_variant = int(variant)
         self._invalidate()
 
     def set_render_resolution(self, new_width: int, new_height: int):

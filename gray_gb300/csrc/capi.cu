@@ -212,6 +212,34 @@ int gray_rebuild_bvh(const gray_params *p, void *stream) {
     return GRAY_OK;
 }
 
+uint32_t gray_batch_packets(uint32_t width, uint32_t height, int32_t variant) {
+    const int v = variant > 0 ? variant : 1;
+    const uint32_t tw = (v & 4) ? 4u : 8u, th = 32u / tw;
+    return ((width + tw - 1) / tw) * ((height + th - 1) / th);
+}
+
+int gray_batch_prep(const gray_params *p, const float *origins, int32_t nviews, float *channels_out, void *stream) {
+    int e = check_common(p);
+    if (e) return e;
+    if (nviews < 0 || (nviews > 0 && (!origins || !channels_out)))
+        return fail(GRAY_ERR_INVALID_ARGUMENT, "batch_prep: bad views");
+    cudaStream_t s = (cudaStream_t)stream;
+    GRAY_LAUNCH("batch_prep", gray::launch_batch_prep(*p, origins, nviews, channels_out, s));
+    return GRAY_OK;
+}
+
+int gray_render_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int32_t nviews,
+                      uint32_t total_packets, float *out, uint32_t *work_counter, int32_t variant,
+                      int32_t blocks_per_sm, int32_t *status, void *stream) {
+    if (nviews <= 0 || !scenes || !views || !out || !work_counter)
+        return fail(GRAY_ERR_INVALID_ARGUMENT, "render_batch: missing buffers");
+    if (blocks_per_sm < 0 || blocks_per_sm > 32) return fail(GRAY_ERR_OUT_OF_RANGE, "render_batch: blocks_per_sm");
+    cudaStream_t s = (cudaStream_t)stream;
+    GRAY_LAUNCH("trace_batch", gray::launch_trace_batch(scenes, views, nviews, total_packets, out, work_counter,
+                                                        variant, blocks_per_sm, status, s));
+    return GRAY_OK;
+}
+
 const char *gray_last_error(void) { return g_last_error.c_str(); }
 
 const char *gray_version(void) { return "gray_gb300 0.1 (sm_103a)"; }

@@ -147,14 +147,15 @@ struct f3 {
 __device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
 __device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
-// Object-space ray of one Gaussian and the max-density point (reference:
-// cuda/shaders.cu:17-49).  g0..g2 = rows (M | mu) of the snapshot.
+// Object-space ray of one Gaussian and its max-density point (reference: cuda/shaders.cu:17-49).
+// g0..g2 = rows (M | mu) of the snapshot.  With lo = M (o - mu) and ld = M d (d a unit world
+// direction), the max-density point is at world distance t = -<lo,ld> / <ld,ld> (the reference
+// normalises ld and divides by its length twice; the value is the same) and u = lo + t ld.
 struct LocalHit {
-    f3 lo, ld;      // object-space origin and (unnormalised) direction
-    float nrm;      // |ld|
-    f3 dn;          // ld / nrm
-    float s;        // distance along dn to the max-density point
-    f3 u;           // max-density point (unit-sphere frame)
+    f3 lo, ld;  // object-space origin and direction
+    float b;    // <lo, ld>
+    float t;    // world distance of the max-density point
+    f3 u;       // max-density point in the unit-sphere frame
 };
 
 __device__ __forceinline__ void local_ray(const float4 g0, const float4 g1, const float4 g2, f3 ro, f3 rd,
@@ -164,13 +165,12 @@ __device__ __forceinline__ void local_ray(const float4 g0, const float4 g1, cons
                g2.x * rel.x + g2.y * rel.y + g2.z * rel.z);
     h.ld = mk3(g0.x * rd.x + g0.y * rd.y + g0.z * rd.z, g1.x * rd.x + g1.y * rd.y + g1.z * rd.z,
                g2.x * rd.x + g2.y * rd.y + g2.z * rd.z);
+    h.b = dot3(h.lo, h.ld);
 }
 
 __device__ __forceinline__ void closest_point(LocalHit &h) {
-    h.nrm = sqrtf(dot3(h.ld, h.ld));
-    h.dn = mk3(h.ld.x / h.nrm, h.ld.y / h.nrm, h.ld.z / h.nrm);
-    h.s = -h.lo.x * h.dn.x + -h.lo.y * h.dn.y + -h.lo.z * h.dn.z;
-    h.u = mk3(h.lo.x + h.s * h.dn.x, h.lo.y + h.s * h.dn.y, h.lo.z + h.s * h.dn.z);
+    h.t = -h.b / dot3(h.ld, h.ld);
+    h.u = mk3(h.lo.x + h.t * h.ld.x, h.lo.y + h.t * h.ld.y, h.lo.z + h.t * h.ld.z);
 }
 
 // Segment [znear, zfar] of the object-space ray against the instance's unit box [-1, 1]^3 (the
@@ -197,11 +197,11 @@ __device__ __forceinline__ bool intersect(const float4 g0, const float4 g1, cons
     if (o <= alpha_threshold) return false;
     LocalHit h;
     local_ray(g0, g1, g2, ro, rd, h);
-    if (dot3(h.lo, h.ld) > 0.0f) return false;
+    if (h.b > 0.0f) return false;
     closest_point(h);
     float sq = dot3(h.u, h.u);
     if (sq > 1.0f) return false;
-    dist = h.s / h.nrm;
+    dist = h.t;
     if (!(dist >= znear && dist <= zfar)) {
         if (!unit_box_overlap(h, znear, zfar)) return false;
     }
@@ -209,6 +209,12 @@ __device__ __forceinline__ bool intersect(const float4 g0, const float4 g1, cons
     float gv = eval_gaussian(dot3(x, x), exp_power);
     alpha = maxalpha_mul(gv, o);
     return true;
+}
+
+// alpha * 2^24 for an fp16 alpha in [0, 1): an exact integer, from the half's bits
+__device__ __forceinline__ long long alpha16_fixed(uint16_t a16) {
+    const uint32_t e = (a16 >> 10) & 0x1fu, m = a16 & 0x3ffu;
+    return e ? (long long)((1024u + m) << (e - 1u)) : (long long)m;
 }
 
 // Device-side error reporting: bits are OR-ed into a status word; the host reads it later.

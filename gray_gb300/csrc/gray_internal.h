@@ -13,6 +13,8 @@ cudaError_t launch_snapshot(const gray_params &p, cudaStream_t s);
 // reset_frame: zero was_visible, count the call and empty the backward hit list (forward_pass)
 cudaError_t launch_forward_prep(const gray_params &p, bool reset_frame, cudaStream_t s);
 cudaError_t launch_fold_and_sh_backward(const gray_params &p, cudaStream_t s);
+cudaError_t launch_batch_prep(const gray_params &p, const float *origins, int nviews, float *channels_out,
+                              cudaStream_t s);
 
 // lbvh.cu
 cudaError_t launch_lbvh_build(const gray_params &p, cudaStream_t s);
@@ -22,6 +24,9 @@ size_t sort_tmp_words(int n);
 // trace.cu
 cudaError_t launch_trace_forward(const gray_params &p, cudaStream_t s);
 cudaError_t launch_trace_backward(const gray_params &p, cudaStream_t s);
+cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int nviews,
+                               uint32_t total_packets, float *out, uint32_t *counter, int variant, int blocks_per_sm,
+                               int32_t *status, cudaStream_t s);
 
 // adam.cu
 cudaError_t launch_adam(const gray_params &p, cudaStream_t s);

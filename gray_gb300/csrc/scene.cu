@@ -263,6 +263,90 @@ cudaError_t launch_forward_prep(const gray_params &p, bool reset_frame, cudaStre
 }
 
 // ---------------------------------------------------------------------------------------------
+// Batched preparation: live values once and the SH colour of every Gaussian for each of
+// `nviews` camera origins (one pass over the SH coefficients serves all views).  Same
+// arithmetic as forward_prep_kernel, so a view's colours are bit-identical to a plain forward.
+// ---------------------------------------------------------------------------------------------
+template <typename SHT>
+__global__ void __launch_bounds__(kPrepThreads) batch_prep_kernel(
+    int n, int num_rest, const float *__restrict__ opacity, const uint8_t *__restrict__ visible,
+    const float *__restrict__ cfg_alpha_threshold, const float *__restrict__ cfg_exp_power,
+    const uint8_t *__restrict__ cfg_enable_sh, const int32_t *__restrict__ current_sh_degree, int max_sh_degree,
+    const float *__restrict__ mean, const float *__restrict__ origins, int nviews, const SHT *__restrict__ sh_dc,
+    const SHT *__restrict__ sh_rest, const float *__restrict__ channels_in, float *__restrict__ channels_out,
+    float2 *__restrict__ live) {
+    extern __shared__ float stage[];
+    const int i0 = blockIdx.x * kPrepThreads;
+    const int i = i0 + threadIdx.x;
+    const bool enable_sh = *cfg_enable_sh != 0;
+    int degree = min(min(*current_sh_degree, 3), max_sh_degree);
+    const int nb = enable_sh ? sh_count(degree) : 0;
+    if (nb > 0) {
+        const int rows = min(kPrepThreads, n - i0);
+        const int per = num_rest * 3;
+        const long long base = (long long)i0 * per;
+        for (int t = threadIdx.x; t < rows * per; t += kPrepThreads) stage[t] = sh_load<SHT>(sh_rest + base + t);
+    }
+    __syncthreads();
+    if (i >= n) return;
+    const float athr = *cfg_alpha_threshold, pw = *cfg_exp_power;
+    float o = sigmoid_act(opacity[i]);
+    float sf = scaling_factor(o, athr, pw);
+    live[i] = make_float2(visible[i] ? o : __int_as_float(0xff800000), sf);
+    const float m0 = mean[3 * i], m1 = mean[3 * i + 1], m2 = mean[3 * i + 2];
+    const float *row = stage + threadIdx.x * num_rest * 3;
+    float dc[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) dc[c] = enable_sh ? sh_load<SHT>(sh_dc + 3 * i + c) : 0.0f;
+    for (int v = 0; v < nviews; v++) {
+        float *out = channels_out + ((size_t)v * n + i) * 3;
+        if (!enable_sh) {
+            out[0] = channels_in[3 * i];
+            out[1] = channels_in[3 * i + 1];
+            out[2] = channels_in[3 * i + 2];
+            continue;
+        }
+        const float v0 = m0 - origins[3 * v], v1 = m1 - origins[3 * v + 1], v2 = m2 - origins[3 * v + 2];
+        float len2 = v0 * v0 + v1 * v1 + v2 * v2;
+        float inv = 1.0f / sqrtf(fmaxf(len2, 1e-20f));
+        float b[15];
+        sh_basis(v0 * inv, v1 * inv, v2 * inv, b);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            float acc = SH_C0 * dc[c];
+#pragma unroll
+            for (int j = 0; j < 15; j++)
+                if (j < nb) acc = fmaf(b[j], row[3 * j + c], acc);
+            acc = acc + 0.5f;
+            out[c] = fmaxf(acc, 0.0f);
+        }
+    }
+}
+
+cudaError_t launch_batch_prep(const gray_params &p, const float *origins, int nviews, float *channels_out,
+                              cudaStream_t s) {
+    const gray_gaussians &g = p.gaussians;
+    if (g.count <= 0 || nviews <= 0) return cudaSuccess;
+    const int num_rest = g.num_sh_coeffs;
+    const size_t smem = (size_t)kPrepThreads * (size_t)(num_rest > 0 ? num_rest : 1) * 3 * sizeof(float);
+    const unsigned int blocks = blocks_for(g.count, kPrepThreads);
+    if (g.sh_is_fp16) {
+        batch_prep_kernel<__half><<<blocks, kPrepThreads, smem, s>>>(
+            g.count, num_rest, g.opacity, p.scene.visible, p.config.alpha_threshold, p.config.exp_power,
+            p.config.enable_sh, g.current_sh_degree, g.max_sh_degree, g.mean, origins, nviews,
+            reinterpret_cast<const __half *>(g.sh_coeffs_dc), reinterpret_cast<const __half *>(g.sh_coeffs_rest),
+            g.channels, channels_out, reinterpret_cast<float2 *>(p.scene.live));
+    } else {
+        batch_prep_kernel<float><<<blocks, kPrepThreads, smem, s>>>(
+            g.count, num_rest, g.opacity, p.scene.visible, p.config.alpha_threshold, p.config.exp_power,
+            p.config.enable_sh, g.current_sh_degree, g.max_sh_degree, g.mean, origins, nviews,
+            reinterpret_cast<const float *>(g.sh_coeffs_dc), reinterpret_cast<const float *>(g.sh_coeffs_rest),
+            g.channels, channels_out, reinterpret_cast<float2 *>(p.scene.live));
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
 // Gradient fold + SH backward.  The trace backward accumulates per-Gaussian gradients with
 // 16-byte vector reductions into grad_acc ([n,16]: rot4 | mean3 opacity | scale3 pruning |
 // channels3 count); this kernel adds them to the reference-layout gradient arrays, sets

@@ -20,21 +20,21 @@
 
 namespace gray {
 
-constexpr int kTileW = 8, kTileH = 4;        // one warp
-constexpr int kBlockWarpsX = 2, kBlockWarpsY = 2;
+constexpr int kBlockWarpsX = 2, kBlockWarpsY = 2;  // 2x2 warp tiles per block
 constexpr int kWarps = kBlockWarpsX * kBlockWarpsY;
-constexpr int kBlockW = kTileW * kBlockWarpsX, kBlockH = kTileH * kBlockWarpsY;
 constexpr int kFwdThreads = kWarps * 32;
 constexpr int kStackWords = 2;               // warp-uniform stack of 64 entries in 2 registers per lane
 constexpr int kStackMax = 32 * kStackWords;
 constexpr int kPassSlots = 32;               // BUFFER_SIZE, cuda/forward_pass.cu:4
 constexpr int kMaxPasses = 99;               // MAX_ITERATIONS, cuda/forward_pass.cu:3
-constexpr int kMaxTraversals = 4 * kMaxPasses;  // bound on re-traversals of one ray
+constexpr int kMaxTraversals = 4 * kMaxPasses * 2;  // bound on re-traversals of one ray
+constexpr int kDefaultTraceVariant = 1;
 constexpr unsigned kFull = 0xffffffffu;
 
 struct FwdArgs {
     uint32_t alloc_w, render_w, render_h;
     int n;
+    int tile_w, tile_h;  // pixels of one warp packet (tile_w * tile_h == 32)
     const float *cam_origin, *fov, *w2c, *znear, *zfar;
     const float *exp_power, *alpha_threshold, *t_threshold, *eps_fwd, *bg;
     const uint8_t *render_depth, *needs_ray_output, *rays_from_python, *jitter, *grads_enabled;
@@ -85,27 +85,54 @@ struct LaneState {
     bool has_resume;
 };
 
+// What one ray traces against.
+struct TraceScene {
+    const float4 *geom;
+    const float2 *live;
+    const float *channels;
+    const float4 *nodes;
+    const float *root_box;
+    int n;
+};
+
+struct TraceKnobs {
+    float znear, zfar, athr, pw, tthr;
+    bool render_depth;
+};
+
+// Backward hit list sink (counter == nullptr: do not record).
+struct HitSink {
+    uint32_t *counter, *pool;
+    uint32_t pool_size;
+};
+
+struct RayResult {
+    float T, C0, C1, C2, depth;
+    LaneState st;
+    int nacc;
+    uint32_t head;
+};
+
 template <int KB>
-__device__ __forceinline__ void on_leaf(const FwdArgs &a, uint32_t gid, bool want, bool first, f3 ro, f3 rd,
-                                        float athr, float pw, float znear, float zfar, LaneState &st,
-                                        unsigned long long (*kbuf)[kFwdThreads]) {
+__device__ __forceinline__ void on_leaf(const TraceScene &sc, uint32_t gid, bool want, bool first, f3 ro, f3 rd,
+                                        const TraceKnobs &k, LaneState &st, unsigned long long (*kbuf)[kFwdThreads]) {
     if (!want) return;
-    const float4 g0 = a.geom[3 * gid], g1 = a.geom[3 * gid + 1], g2 = a.geom[3 * gid + 2];
-    const float2 lv = a.live[gid];
+    const float4 g0 = sc.geom[3 * gid], g1 = sc.geom[3 * gid + 1], g2 = sc.geom[3 * gid + 2];
+    const float2 lv = sc.live[gid];
     float dist, alpha;
-    if (!intersect(g0, g1, g2, lv.x, lv.y, ro, rd, athr, pw, znear, zfar, dist, alpha)) return;
+    if (!intersect(g0, g1, g2, lv.x, lv.y, ro, rd, k.athr, k.pw, k.znear, k.zfar, dist, alpha)) return;
     const uint16_t a16 = f2h_bits(alpha), d16 = f2h_bits(dist);
     if (first) {
         st.ft = fmaf(-st.ft, alpha, st.ft);
         const float af = h2f_bits(a16);
-        const float *c = a.channels + 3 * (size_t)gid;
-        st.afx += to_fixed(af, 0x1.0p24f);
+        const float *c = sc.channels + 3 * (size_t)gid;
+        st.afx += alpha16_fixed(a16);
         st.cfx0 += to_fixed(af * c[0], 0x1.0p32f);
         st.cfx1 += to_fixed(af * c[1], 0x1.0p32f);
         st.cfx2 += to_fixed(af * c[2], 0x1.0p32f);
         st.nhit++;
     }
-    if (!(h2f_bits(d16) > znear)) return;
+    if (!(h2f_bits(d16) > k.znear)) return;
     const unsigned long long key =
         ((unsigned long long)d16 << 48) | ((unsigned long long)gid << 16) | (unsigned long long)a16;
     if (st.has_resume && !(key > st.resume)) return;
@@ -129,48 +156,28 @@ __device__ __forceinline__ void on_leaf(const FwdArgs &a, uint32_t gid, bool wan
     if (st.kcount == KB) st.kmax = kbuf[KB - 1][t];
 }
 
-template <int KB>
-__global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArgs a) {
-    __shared__ unsigned long long kbuf[KB][kFwdThreads];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int px = blockIdx.x * kBlockW + (warp % kBlockWarpsX) * kTileW + (lane % kTileW);
-    const int py = blockIdx.y * kBlockH + (warp / kBlockWarpsX) * kTileH + (lane / kTileW);
-    const bool inside = px < (int)a.render_w && py < (int)a.render_h;
-    const uint32_t pixel = (uint32_t)py * a.alloc_w + (uint32_t)px;
-
-    const float znear = *a.znear, zfar = *a.zfar;
-    const float athr = *a.alpha_threshold, pw = *a.exp_power, tthr = *a.t_threshold;
-    const bool grads = *a.grads_enabled != 0;
-    const bool render_depth = *a.render_depth != 0;
-
-    // ---- ray generation (cuda/shaders.cu:76-88, cuda/core/camera.h:17-36) ----
-    f3 ro = mk3(0.0f, 0.0f, 0.0f), rd = mk3(0.0f, 0.0f, 0.0f);
-    bool alive = false;
-    if (inside) {
-        if (*a.rays_from_python) {
-            ro = mk3(a.ray_o[3 * pixel], a.ray_o[3 * pixel + 1], a.ray_o[3 * pixel + 2]);
-            rd = mk3(a.ray_d[3 * pixel], a.ray_d[3 * pixel + 1], a.ray_d[3 * pixel + 2]);
-        } else {
-            ro = mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]);
-            const float view_size = tanf(*a.fov / 2.0f);
-            const float aspect = (float)a.render_w / (float)a.render_h;
-            float fx = (float)px, fy = (float)py;
-            if (*a.jitter) {
-                uint32_t h = pcg_hash(pixel ^ pcg_hash(*a.total_num_calls));
-                fx = fx + ((float)(h & 0xFFFFu) * 0x1.0p-16f - 0.5f);
-                fy = fy + ((float)(h >> 16) * 0x1.0p-16f - 0.5f);
-            }
-            const float y = view_size * (1.0f - 2.0f * (fy + 0.5f) / (float)a.render_h);
-            const float x = aspect * view_size * (2.0f * (fx + 0.5f) / (float)a.render_w - 1.0f);
-            const float *w = a.w2c;
-            f3 v = mk3(w[0] * x + w[3] * y - w[6], w[1] * x + w[4] * y - w[7], w[2] * x + w[5] * y - w[8]);
-            const float inv = 1.0f / sqrtf(dot3(v, v));
-            rd = mk3(v.x * inv, v.y * inv, v.z * inv);
+__device__ __forceinline__ void stack_push(uint32_t &stk0, uint32_t &stk1, int &sp, uint32_t v, int lane,
+                                           int32_t *status) {
+    if (sp < kStackMax) {
+        if (lane == (sp & 31)) {
+            if ((sp >> 5) == 0) stk0 = v;
+            else stk1 = v;
         }
-        alive = !(sqrtf(dot3(rd, rd)) == 0.0f);
+        sp++;
+    } else {
+        raise_status(status, GRAY_STATUS_STACK_OVERFLOW);
     }
+}
 
-    LaneState st;
+// Trace the warp's 32 rays (one per lane; `alive` lanes only) through the scene: traversal,
+// selection, compositing (cuda/forward_pass.cu:6-151 minus the write-out).  Every lane of the
+// warp must call this together.
+template <int KB>
+__device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool alive,
+                                          bool grads, const HitSink &hs, int32_t *status,
+                                          unsigned long long (*kbuf)[kFwdThreads], RayResult &res) {
+    const int lane = threadIdx.x & 31;
+    LaneState &st = res.st;
     st.ft = 1.0f;
     st.afx = st.cfx0 = st.cfx1 = st.cfx2 = 0;
     st.nhit = 0;
@@ -181,11 +188,11 @@ __global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArg
     st.has_resume = false;
     float T = 1.0f, C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, depth = 0.0f;
     int pass = 0, slots = 0, nacc = 0;
-    float tmin_sel = znear, last_d = znear;
+    float tmin_sel = k.znear, last_d = k.znear;
     bool done = !alive;
     uint32_t head = GRAY_NULL;
 
-    f3 inv = mk3(0.0f, 0.0f, 0.0f);
+    f3 inv;
     {
         float dx = fabsf(rd.x) < 1e-20f ? (rd.x < 0.0f ? -1e-20f : 1e-20f) : rd.x;
         float dy = fabsf(rd.y) < 1e-20f ? (rd.y < 0.0f ? -1e-20f : 1e-20f) : rd.y;
@@ -204,22 +211,22 @@ __global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArg
 
     bool first = true;
     int traversals = 0;
-    const int n = a.n;
+    const int n = sc.n;
     while (__any_sync(kFull, !done)) {
         const bool want = !done;
         st.kcount = 0;
         st.ncand = 0;
         // ---------------- traversal ----------------
         if (n == 1) {
-            const float *rb = a.root_box;
+            const float *rb = sc.root_box;
             const float bmin[3] = {rb[0], rb[1], rb[2]}, bmax[3] = {rb[4], rb[5], rb[6]};
             bool h = want && slab_hit(bmin, bmax, ro, inv, eps);
-            if (__any_sync(kFull, h)) on_leaf<KB>(a, 0u, h, first, ro, rd, athr, pw, znear, zfar, st, kbuf);
+            if (__any_sync(kFull, h)) on_leaf<KB>(sc, 0u, h, first, ro, rd, k, st, kbuf);
         } else if (n > 1) {
             uint32_t stk0 = 0, stk1 = 0;  // entry e lives in lane e%32, word e/32
             int sp = 0;
             {
-                const float *rb = a.root_box;
+                const float *rb = sc.root_box;
                 const float bmin[3] = {rb[0], rb[1], rb[2]}, bmax[3] = {rb[4], rb[5], rb[6]};
                 bool h = want && slab_hit(bmin, bmax, ro, inv, eps);
                 if (__any_sync(kFull, h)) {
@@ -232,11 +239,11 @@ __global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArg
                 const uint32_t word = (sp >> 5) == 0 ? stk0 : stk1;
                 const uint32_t node = __shfl_sync(kFull, word, sp & 31);
                 if (node >= (uint32_t)(n - 1)) {
-                    raise_status(a.status, GRAY_STATUS_STACK_OVERFLOW);
+                    raise_status(status, GRAY_STATUS_STACK_OVERFLOW);
                     continue;
                 }
-                const float4 q0 = a.nodes[4 * node], q1 = a.nodes[4 * node + 1], q2 = a.nodes[4 * node + 2],
-                             q3 = a.nodes[4 * node + 3];
+                const float4 q0 = sc.nodes[4 * node], q1 = sc.nodes[4 * node + 1], q2 = sc.nodes[4 * node + 2],
+                             q3 = sc.nodes[4 * node + 3];
                 const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
                 const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
                 const uint32_t c0 = __float_as_uint(q3.x), c1 = __float_as_uint(q3.y);
@@ -253,36 +260,16 @@ __global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArg
                 const bool hn = swap ? h1 : h0, hf = swap ? h0 : h1;
                 // far internal child goes deeper in the stack, near internal child on top;
                 // leaves are processed right away, near first
-                if (af && !(cf & GRAY_LEAF_BIT)) {
-                    if (sp < kStackMax) {
-                        if (lane == (sp & 31)) {
-                            if ((sp >> 5) == 0) stk0 = cf;
-                            else stk1 = cf;
-                        }
-                        sp++;
-                    } else {
-                        raise_status(a.status, GRAY_STATUS_STACK_OVERFLOW);
-                    }
-                }
+                if (af && !(cf & GRAY_LEAF_BIT)) stack_push(stk0, stk1, sp, cf, lane, status);
                 if (an && (cn & GRAY_LEAF_BIT)) {
                     const uint32_t gid = cn & ~GRAY_LEAF_BIT;
-                    if (gid < (uint32_t)n) on_leaf<KB>(a, gid, hn, first, ro, rd, athr, pw, znear, zfar, st, kbuf);
+                    if (gid < (uint32_t)n) on_leaf<KB>(sc, gid, hn, first, ro, rd, k, st, kbuf);
                 }
                 if (af && (cf & GRAY_LEAF_BIT)) {
                     const uint32_t gid = cf & ~GRAY_LEAF_BIT;
-                    if (gid < (uint32_t)n) on_leaf<KB>(a, gid, hf, first, ro, rd, athr, pw, znear, zfar, st, kbuf);
+                    if (gid < (uint32_t)n) on_leaf<KB>(sc, gid, hf, first, ro, rd, k, st, kbuf);
                 }
-                if (an && !(cn & GRAY_LEAF_BIT)) {
-                    if (sp < kStackMax) {
-                        if (lane == (sp & 31)) {
-                            if ((sp >> 5) == 0) stk0 = cn;
-                            else stk1 = cn;
-                        }
-                        sp++;
-                    } else {
-                        raise_status(a.status, GRAY_STATUS_STACK_OVERFLOW);
-                    }
-                }
+                if (an && !(cn & GRAY_LEAF_BIT)) stack_push(stk0, stk1, sp, cn, lane, status);
             }
         }
         // ---------------- consume (cuda/forward_pass.cu:46-125) ----------------
@@ -301,7 +288,7 @@ __global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArg
                         break;
                     }
                     tmin_sel = last_d;
-                    if (!(tmin_sel < zfar)) {
+                    if (!(tmin_sel < k.zfar)) {
                         done = true;
                         break;
                     }
@@ -310,15 +297,15 @@ __global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArg
                 }
                 slots++;
                 last_d = d;
-                if (!(d < zfar)) {
+                if (!(d < k.zfar)) {
                     done = true;
                     break;
                 }
                 const uint32_t gid = (uint32_t)(key >> 16);
                 const float al = h2f_bits((uint16_t)(key & 0xFFFFu));
-                const float *c = a.channels + 3 * (size_t)gid;
+                const float *c = sc.channels + 3 * (size_t)gid;
                 const float cx = c[0], cy = c[1], cz = c[2];
-                st.afx -= to_fixed(al, 0x1.0p24f);
+                st.afx -= alpha16_fixed((uint16_t)(key & 0xFFFFu));
                 st.cfx0 -= to_fixed(al * cx, 0x1.0p32f);
                 st.cfx1 -= to_fixed(al * cy, 0x1.0p32f);
                 st.cfx2 -= to_fixed(al * cz, 0x1.0p32f);
@@ -326,12 +313,12 @@ __global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArg
                 C0 = C0 + cx * w;
                 C1 = C1 + cy * w;
                 C2 = C2 + cz * w;
-                if (render_depth) depth = depth + d * w;
+                if (k.render_depth) depth = depth + d * w;
                 T = T * (1.0f - al);
                 kbuf[nc][t] = gid;
                 nc++;
                 nacc++;
-                if (T < tthr) {
+                if (T < k.tthr) {
                     done = true;
                     break;
                 }
@@ -350,7 +337,7 @@ __global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArg
                     st.resume = r;
                     st.has_resume = true;
                     if (++traversals > kMaxTraversals) {
-                        raise_status(a.status, GRAY_STATUS_STACK_OVERFLOW);
+                        raise_status(status, GRAY_STATUS_STACK_OVERFLOW);
                         done = true;
                     }
                 } else {
@@ -370,54 +357,124 @@ __global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArg
             const uint32_t total = __shfl_sync(kFull, incl, 31);
             uint32_t base = 0;
             if (total > 0) {
-                if (lane == 31) base = atomicAdd(a.counter, total);
+                if (lane == 31) base = atomicAdd(hs.counter, total);
                 base = __shfl_sync(kFull, base, 31);
             }
             if (need > 0) {
                 const uint32_t off = base + incl - need;
-                const bool fits = base <= a.pool_size && total <= a.pool_size - base;
+                const bool fits = base <= hs.pool_size && total <= hs.pool_size - base;
                 if (fits) {
-                    a.pool[off] = head;
-                    a.pool[off + 1] = (uint32_t)nc;
-                    for (int j = 0; j < nc; j++) a.pool[off + 2 + j] = (uint32_t)kbuf[j][threadIdx.x];
+                    hs.pool[off] = head;
+                    hs.pool[off + 1] = (uint32_t)nc;
+                    for (int j = 0; j < nc; j++) hs.pool[off + 2 + j] = (uint32_t)kbuf[j][threadIdx.x];
                     head = off;
                 } else {
-                    raise_status(a.status, GRAY_STATUS_HITLIST_OVERFLOW);
+                    raise_status(status, GRAY_STATUS_HITLIST_OVERFLOW);
                 }
             }
         }
         first = false;
     }
+    res.T = T;
+    res.C0 = C0;
+    res.C1 = C1;
+    res.C2 = C2;
+    res.depth = depth;
+    res.nacc = nacc;
+    res.head = head;
+}
 
-    if (!inside) return;
-    if (!alive) {
-        a.head[pixel] = GRAY_NULL;  // inactive pixel: empty list, nothing else written
-        return;
-    }
-    // ---------------- truncated-tail estimate, background, write-out ----------------
-    const float rT = T - st.ft;
-    float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+// Truncated-tail estimate and background (cuda/forward_pass.cu:131-142).
+__device__ __forceinline__ void finish_ray(RayResult &r, const float *bg, float eps_fwd, bool render_depth,
+                                           float &r0, float &r1, float &r2) {
+    const LaneState &st = r.st;
+    const float rT = r.T - st.ft;
+    r0 = r1 = r2 = 0.0f;
     if (st.afx > 0) {
         const float sa = __ll2float_rn(st.afx) * 0x1.0p-24f;
         r0 = (__ll2float_rn(st.cfx0) * 0x1.0p-32f) / sa;
         r1 = (__ll2float_rn(st.cfx1) * 0x1.0p-32f) / sa;
         r2 = (__ll2float_rn(st.cfx2) * 0x1.0p-32f) / sa;
     }
-    C0 = C0 + rT * r0;
-    C1 = C1 + rT * r1;
-    C2 = C2 + rT * r2;
-    if (render_depth) depth = depth / fmaxf(1.0f - T, *a.eps_fwd);
-    const float *bg = a.bg;
-    C0 = C0 + bg[0] * st.ft;
-    C1 = C1 + bg[1] * st.ft;
-    C2 = C2 + bg[2] * st.ft;
-    a.out_rgb[3 * pixel] = C0;
-    a.out_rgb[3 * pixel + 1] = C1;
-    a.out_rgb[3 * pixel + 2] = C2;
+    r.C0 = r.C0 + rT * r0;
+    r.C1 = r.C1 + rT * r1;
+    r.C2 = r.C2 + rT * r2;
+    if (render_depth) r.depth = r.depth / fmaxf(1.0f - r.T, eps_fwd);
+    r.C0 = r.C0 + bg[0] * st.ft;
+    r.C1 = r.C1 + bg[1] * st.ft;
+    r.C2 = r.C2 + bg[2] * st.ft;
+}
+
+// Primary ray of pixel (px, py) of a width x height pinhole camera (cuda/core/camera.h:17-36).
+__device__ __forceinline__ f3 camera_ray(const float *w, float fov, int px, int py, uint32_t width, uint32_t height,
+                                         float jx, float jy) {
+    const float view_size = tanf(fov / 2.0f);
+    const float aspect = (float)width / (float)height;
+    const float fx = (float)px + jx, fy = (float)py + jy;
+    const float y = view_size * (1.0f - 2.0f * (fy + 0.5f) / (float)height);
+    const float x = aspect * view_size * (2.0f * (fx + 0.5f) / (float)width - 1.0f);
+    f3 v = mk3(w[0] * x + w[3] * y - w[6], w[1] * x + w[4] * y - w[7], w[2] * x + w[5] * y - w[8]);
+    const float inv = 1.0f / sqrtf(dot3(v, v));
+    return mk3(v.x * inv, v.y * inv, v.z * inv);
+}
+
+template <int KB, int MINB>
+__global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const FwdArgs a) {
+    __shared__ unsigned long long kbuf[KB][kFwdThreads];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int px = blockIdx.x * (a.tile_w * kBlockWarpsX) + (warp % kBlockWarpsX) * a.tile_w + (lane % a.tile_w);
+    const int py = blockIdx.y * (a.tile_h * kBlockWarpsY) + (warp / kBlockWarpsX) * a.tile_h + (lane / a.tile_w);
+    const bool inside = px < (int)a.render_w && py < (int)a.render_h;
+    const uint32_t pixel = (uint32_t)py * a.alloc_w + (uint32_t)px;
+
+    TraceKnobs k;
+    k.znear = *a.znear;
+    k.zfar = *a.zfar;
+    k.athr = *a.alpha_threshold;
+    k.pw = *a.exp_power;
+    k.tthr = *a.t_threshold;
+    k.render_depth = *a.render_depth != 0;
+    const bool grads = *a.grads_enabled != 0;
+    const TraceScene sc{a.geom, a.live, a.channels, a.nodes, a.root_box, a.n};
+    const HitSink hs{a.counter, a.pool, a.pool_size};
+
+    // ---- ray generation (cuda/shaders.cu:76-88) ----
+    f3 ro = mk3(0.0f, 0.0f, 0.0f), rd = mk3(0.0f, 0.0f, 0.0f);
+    bool alive = false;
+    if (inside) {
+        if (*a.rays_from_python) {
+            ro = mk3(a.ray_o[3 * pixel], a.ray_o[3 * pixel + 1], a.ray_o[3 * pixel + 2]);
+            rd = mk3(a.ray_d[3 * pixel], a.ray_d[3 * pixel + 1], a.ray_d[3 * pixel + 2]);
+        } else {
+            ro = mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]);
+            float jx = 0.0f, jy = 0.0f;
+            if (*a.jitter) {
+                uint32_t h = pcg_hash(pixel ^ pcg_hash(*a.total_num_calls));
+                jx = (float)(h & 0xFFFFu) * 0x1.0p-16f - 0.5f;
+                jy = (float)(h >> 16) * 0x1.0p-16f - 0.5f;
+            }
+            rd = camera_ray(a.w2c, *a.fov, px, py, a.render_w, a.render_h, jx, jy);
+        }
+        alive = !(sqrtf(dot3(rd, rd)) == 0.0f);
+    }
+
+    RayResult r;
+    trace_ray<KB>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r);
+
+    if (!inside) return;
+    if (!alive) {
+        a.head[pixel] = GRAY_NULL;  // inactive pixel: empty list, nothing else written
+        return;
+    }
+    float r0, r1, r2;
+    finish_ray(r, a.bg, *a.eps_fwd, k.render_depth, r0, r1, r2);
+    a.out_rgb[3 * pixel] = r.C0;
+    a.out_rgb[3 * pixel + 1] = r.C1;
+    a.out_rgb[3 * pixel + 2] = r.C2;
     if (grads) {
-        a.out_depth[pixel] = depth;
-        a.out_T[pixel] = T;
-        a.out_fullT[pixel] = st.ft;
+        a.out_depth[pixel] = r.depth;
+        a.out_T[pixel] = r.T;
+        a.out_fullT[pixel] = r.st.ft;
         a.out_rem[3 * pixel] = r0;
         a.out_rem[3 * pixel + 1] = r1;
         a.out_rem[3 * pixel + 2] = r2;
@@ -427,18 +484,70 @@ __global__ void __launch_bounds__(kFwdThreads) trace_forward_kernel(const FwdArg
         a.ray_d[3 * pixel] = rd.x;
         a.ray_d[3 * pixel + 1] = rd.y;
         a.ray_d[3 * pixel + 2] = rd.z;
-        a.stat_hit[pixel] += st.nhit;
-        a.stat_acc[pixel] += nacc;
-        a.head[pixel] = head;
+        a.stat_hit[pixel] += r.st.nhit;
+        a.stat_acc[pixel] += r.nacc;
+        a.head[pixel] = r.head;
     } else {
         const bool nro = *a.needs_ray_output != 0;
-        if (render_depth || nro) a.out_depth[pixel] = depth;
+        if (k.render_depth || nro) a.out_depth[pixel] = r.depth;
         if (nro) {
             a.ray_d[3 * pixel] = rd.x;
             a.ray_d[3 * pixel + 1] = rd.y;
             a.ray_d[3 * pixel + 2] = rd.z;
         }
         a.head[pixel] = GRAY_NULL;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Batched render: many views (of one or several resident scenes) in one persistent launch.
+// Warps pull 32-ray packets from a global counter; packet -> (view, tile) through the views'
+// packet offsets.  Forward only (no gradients, no hit lists); per view the output is RGB.
+// ---------------------------------------------------------------------------------------------
+template <int KB, int MINB>
+__global__ void __launch_bounds__(kFwdThreads, MINB)
+    trace_batch_kernel(const gray_batch_scene *__restrict__ scenes, const gray_batch_view *__restrict__ views,
+                       int nviews, uint32_t total_packets, float *__restrict__ out, uint32_t *__restrict__ counter,
+                       int tile_w, int32_t *status) {
+    __shared__ unsigned long long kbuf[KB][kFwdThreads];
+    const int lane = threadIdx.x & 31;
+    const int tile_h = 32 / tile_w;
+    for (;;) {
+        uint32_t packet = 0;
+        if (lane == 0) packet = atomicAdd(counter, 1u);
+        packet = __shfl_sync(kFull, packet, 0);
+        if (packet >= total_packets) break;
+        int v = 0;
+        while (v + 1 < nviews && views[v + 1].packet_offset <= packet) v++;
+        const gray_batch_view &vw = views[v];
+        const gray_batch_scene &bs = scenes[vw.scene];
+        const uint32_t local = packet - vw.packet_offset;
+        const uint32_t tiles_x = (vw.width + tile_w - 1) / tile_w;
+        const int px = (int)((local % tiles_x) * tile_w) + lane % tile_w;
+        const int py = (int)((local / tiles_x) * tile_h) + lane / tile_w;
+        const bool inside = px < (int)vw.width && py < (int)vw.height;
+        TraceKnobs k;
+        k.znear = vw.znear;
+        k.zfar = vw.zfar;
+        k.athr = bs.alpha_threshold;
+        k.pw = bs.exp_power;
+        k.tthr = bs.t_threshold;
+        k.render_depth = false;
+        const TraceScene sc{reinterpret_cast<const float4 *>(bs.geom), reinterpret_cast<const float2 *>(bs.live),
+                            vw.channels, reinterpret_cast<const float4 *>(bs.nodes), bs.root_box, bs.n};
+        const HitSink hs{nullptr, nullptr, 0};
+        f3 ro = mk3(vw.origin[0], vw.origin[1], vw.origin[2]);
+        f3 rd = mk3(0.0f, 0.0f, 0.0f);
+        if (inside) rd = camera_ray(vw.w2c, vw.fov_y, px, py, vw.width, vw.height, 0.0f, 0.0f);
+        RayResult r;
+        trace_ray<KB>(sc, k, ro, rd, inside, false, hs, status, kbuf, r);
+        if (!inside) continue;
+        float r0, r1, r2;
+        finish_ray(r, bs.bg, 1e-12f, false, r0, r1, r2);
+        float *o = out + vw.out_offset + 3 * ((size_t)py * vw.width + px);
+        o[0] = r.C0;
+        o[1] = r.C1;
+        o[2] = r.C2;
     }
 }
 
@@ -483,8 +592,38 @@ cudaError_t launch_trace_forward(const gray_params &p, cudaStream_t s) {
     a.pool = p.hitlist.pool;
     a.pool_size = p.hitlist.size;
     a.status = p.status;
-    dim3 grid((p.render_width + kBlockW - 1) / kBlockW, (p.render_height + kBlockH - 1) / kBlockH);
-    trace_forward_kernel<kPassSlots><<<grid, kFwdThreads, 0, s>>>(a);
+    // variant: bits 0-1 select (buffer size, register cap), bit 2 the packet shape
+    const int v = p.trace_variant > 0 ? p.trace_variant : kDefaultTraceVariant;
+    a.tile_w = (v & 4) ? 4 : 8;
+    a.tile_h = 32 / a.tile_w;
+    const int bw = a.tile_w * kBlockWarpsX, bh = a.tile_h * kBlockWarpsY;
+    dim3 grid((p.render_width + bw - 1) / bw, (p.render_height + bh - 1) / bh);
+    switch (v & 3) {
+        case 0: trace_forward_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(a); break;
+        case 1: trace_forward_kernel<32, 6><<<grid, kFwdThreads, 0, s>>>(a); break;
+        case 2: trace_forward_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(a); break;
+        default: trace_forward_kernel<16, 8><<<grid, kFwdThreads, 0, s>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int nviews,
+                               uint32_t total_packets, float *out, uint32_t *counter, int variant, int blocks_per_sm,
+                               int32_t *status, cudaStream_t s) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const int v = variant > 0 ? variant : kDefaultTraceVariant;
+    const int tile_w = (v & 4) ? 4 : 8;
+    const unsigned int grid = (unsigned int)(sms * (blocks_per_sm > 0 ? blocks_per_sm : 4));
+    if ((e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
+    switch (v & 3) {
+        case 0: trace_batch_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
+        case 1: trace_batch_kernel<32, 6><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
+        case 2: trace_batch_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
+        default: trace_batch_kernel<16, 8><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
+    }
     return cudaGetLastError();
 }
 
@@ -555,7 +694,7 @@ __global__ void __launch_bounds__(128) trace_backward_kernel(const BwdArgs a) {
             LocalHit h;
             local_ray(g0, g1, g2, ro, rd, h);
             closest_point(h);
-            const f3 x = mk3((h.lo.x + h.s * h.dn.x) * sf, (h.lo.y + h.s * h.dn.y) * sf, (h.lo.z + h.s * h.dn.z) * sf);
+            const f3 x = mk3(h.u.x * sf, h.u.y * sf, h.u.z * sf);
             const float sq = dot3(x, x);
             const float gv = eval_gaussian(sq, pw);
             const float alpha = maxalpha_mul(gv, o);

@@ -156,7 +156,52 @@ typedef struct gray_params {
     gray_hitlist hitlist;
     gray_scene scene;
     int32_t *status; /* device int32, GRAY_STATUS_* bits */
+    /* forward-trace kernel variant (0 = library default): bits 0-1 = physical hit buffer of
+     * 32 or 16 keys and register cap, bit 2 = 8x4 or 4x8 pixel packets.  Results are identical
+     * for every variant; only speed differs (see gray_gb300.autotune). */
+    int32_t trace_variant;
 } gray_params;
+
+/* ---- batched rendering (many views, one persistent launch) ----
+ * No reference counterpart: the reference renders one view per OptiX launch
+ * (cuda/raytracer.h:104-114 forward_pass_display).  A batch renders any number of views of one or
+ * several resident scenes, each at its own resolution, forward only (inference), in one launch
+ * whose warps pull 32-ray packets from a global counter.  Per pixel the result is bit-identical to
+ * gray_forward_pass_display of the same view. */
+typedef struct gray_batch_scene {
+    const float *geom, *live, *nodes, *root_box; /* a scene's gray_scene buffers after rebuild/update */
+    int32_t n;                                   /* Gaussian count */
+    float exp_power, alpha_threshold, t_threshold;
+    float bg[3];
+    int32_t pad;
+} gray_batch_scene;
+
+typedef struct gray_batch_view {
+    float origin[3];
+    float w2c[9];          /* rows = camera axes (rotation_w2c of CameraDataHolder) */
+    float fov_y, znear, zfar;
+    uint32_t width, height;
+    uint32_t scene;        /* index into the scene table */
+    uint32_t packet_offset;/* first packet of this view; views in increasing order */
+    uint32_t pad;
+    uint64_t out_offset;   /* float index of pixel (0,0): RGB, row-major, width x height */
+    const float *channels; /* [n,3] colours of the view's scene for this view (gray_batch_prep) */
+} gray_batch_view;
+
+/* Packets (32-ray tiles) of a width x height view for a kernel variant. */
+uint32_t gray_batch_packets(uint32_t width, uint32_t height, int32_t variant);
+
+/* Per-view colours of one scene: live values (as forward_pass_display) and, when enable_sh, the SH
+ * colour of every Gaussian for each of the nviews camera origins (device [nviews,3]) into
+ * channels_out (device [nviews,n,3]); without SH the scene's channels are copied per view. */
+int gray_batch_prep(const gray_params *p, const float *origins, int32_t nviews, float *channels_out, void *stream);
+
+/* Render the views (device arrays scenes[], views[]) into out; work_counter is one device word
+ * the launch resets and consumes; variant as gray_params.trace_variant; blocks_per_sm sizes the
+ * persistent grid (0 = 4). */
+int gray_render_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int32_t nviews,
+                      uint32_t total_packets, float *out, uint32_t *work_counter, int32_t variant,
+                      int32_t blocks_per_sm, int32_t *status, void *stream);
 
 /* Workspace sizes in 32-bit words for n Gaussians: sort_tmp_words. */
 size_t gray_sort_tmp_words(int32_t n);

@@ -606,14 +606,14 @@ static inline is_result intersect(const float *g, float o, float sf, const float
         lo[r] = m[0] * rel[0] + m[1] * rel[1] + m[2] * rel[2];
         ld[r] = m[0] * rd[0] + m[1] * rd[1] + m[2] * rd[2];
     }
-    if (lo[0] * ld[0] + lo[1] * ld[1] + lo[2] * ld[2] > 0.0f) return res;
-    float nrm = sqrtf(ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
-    float dn[3] = {ld[0] / nrm, ld[1] / nrm, ld[2] / nrm};
-    float s = -lo[0] * dn[0] + -lo[1] * dn[1] + -lo[2] * dn[2];
-    float u[3] = {lo[0] + s * dn[0], lo[1] + s * dn[1], lo[2] + s * dn[2]};
+    /* world distance of the max-density point: t = -<lo,ld>/<ld,ld> (d is a unit vector) */
+    float b = lo[0] * ld[0] + lo[1] * ld[1] + lo[2] * ld[2];
+    if (b > 0.0f) return res;
+    float t = -b / (ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
+    float u[3] = {lo[0] + t * ld[0], lo[1] + t * ld[1], lo[2] + t * ld[2]};
     float sq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
     if (sq > 1.0f) return res;
-    float dist = s / nrm;
+    float dist = t;
     if (!(dist >= cfg->znear && dist <= cfg->zfar)) {
         /* the ray segment [znear, zfar] must still touch the instance's unit box (OptiX AABB test) */
         float t0 = cfg->znear, t1 = cfg->zfar;
@@ -929,11 +929,10 @@ static void backward_range(const bwd_job *J) {
                 lo[k] = m[0] * rel[0] + m[1] * rel[1] + m[2] * rel[2];
                 ld[k] = m[0] * rd[0] + m[1] * rd[1] + m[2] * rd[2];
             }
-            float nrm = sqrtf(ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
-            float dn[3] = {ld[0] / nrm, ld[1] / nrm, ld[2] / nrm};
-            float sd = -lo[0] * dn[0] + -lo[1] * dn[1] + -lo[2] * dn[2];
+            float b = lo[0] * ld[0] + lo[1] * ld[1] + lo[2] * ld[2];
+            float td = -b / (ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
             float x[3];
-            for (int k = 0; k < 3; k++) x[k] = (lo[k] + sd * dn[k]) * sf;
+            for (int k = 0; k < 3; k++) x[k] = (lo[k] + td * ld[k]) * sf;
             float sq = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
             float gv = eval_gaussian(sq, cfg->exp_power);
             float alpha = orc_maxalpha_mul(gv, o);

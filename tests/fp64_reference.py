@@ -1,7 +1,7 @@
 """Differentiable FP64 torch restatement of the reference's compositing rule (test infrastructure).
 
-Follows cuda/shaders.cu:10-67 and cuda/forward_pass.cu:6-151 without the fp16 quantisation of the
-per-pixel list: per (ray, Gaussian) the max-density point, the hit test (in front of the origin,
+Follows cuda/shaders.cu:10-67 and cuda/forward_pass.cu:6-151 with the hits ordered by their fp16
+distance like the reference's per-pixel list but with exact (unquantised) alpha: per (ray, Gaussian) the max-density point, the hit test (in front of the origin,
 inside the clipped unit sphere), alpha = 0.9999 * sigmoid(opacity) * exp(-|x|^4 / 4) (exp_power 2),
 hits composited front to back until T < t_threshold, full transmittance over all hits, and the
 detached tail estimate of the skipped hits.  Used as the smooth function for finite differences and
@@ -48,13 +48,18 @@ def render(ray_o, ray_d, mean, rotation, log_scale, logit_opacity, channels, alp
         hit = ((lo * ld).sum(-1) <= 0) & (d <= sf[None, :] ** 2) & (o[None, :] > alpha_threshold)
         alpha = MAX_ALPHA * o[None, :] * torch.exp(-0.25 * d * d)
         alpha = torch.where(hit, alpha, torch.zeros_like(alpha))
-        order = torch.argsort(torch.where(hit, t, torch.full_like(t, math.inf)).detach(), dim=-1)
+        # the reference orders hits by their fp16-rounded distance (cuda/core/per_pixel_linked_list.h:29);
+        # equal keys keep gaussian-id order (stable sort), and only keys > znear (0) are composited
+        t16 = t.detach().to(torch.float16).to(t.dtype)
+        key = torch.where(hit, t16, torch.full_like(t16, math.inf))
+        order = torch.argsort(key, dim=-1, stable=True)
+        selectable = torch.gather(hit & (t16 > 0), 1, order)
         a_s = torch.gather(alpha, 1, order)
         c_s = channels[order]                                        # [r,N,3]
         one_minus = 1.0 - a_s
-        T_after = torch.cumprod(one_minus, dim=-1)
+        T_after = torch.cumprod(torch.where(selectable, one_minus, torch.ones_like(one_minus)), dim=-1)
         T_before = torch.cat([torch.ones_like(T_after[:, :1]), T_after[:, :-1]], dim=-1)
-        comp = (T_before.detach() >= t_threshold) & (a_s.detach() > 0)
+        comp = (T_before.detach() >= t_threshold) & selectable
         w = torch.where(comp, T_before * a_s, torch.zeros_like(a_s))
         C = (w[..., None] * c_s).sum(1)
         T_fin = torch.prod(torch.where(comp, one_minus, torch.ones_like(one_minus)), dim=-1)

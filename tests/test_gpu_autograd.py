@@ -60,9 +60,10 @@ def test_gradients_vs_fp64_and_finite_differences():
         out = F64.render(ro, rd, ps[0], ps[1], ps[2], ps[3], ps[4])
         return (out.reshape(128, 128, 3).permute(2, 0, 1) * wgt).sum()
 
-    # the GPU image against the FP64 rule: fp16 alpha quantisation bound
+    # the GPU image against the FP64 rule: the difference is the fp16 quantisation of alpha
     ref_img = F64.render(ro, rd, *[t.detach() for t in p64]).reshape(128, 128, 3).permute(2, 0, 1)
-    assert (img.double() - ref_img).abs().max().item() < 5e-3
+    diff = (img.double() - ref_img).abs()
+    assert diff.mean().item() < 1e-4 and diff.max().item() < 2e-3, (diff.mean().item(), diff.max().item())
     l64 = loss64(p64)
     g64 = torch.autograd.grad(l64, p64)
     names = ("mean", "rotation", "scale", "opacity", "channels")

@@ -343,3 +343,22 @@ def test_clustered_scene_with_bvh(oracle):
     fwd = oracle.trace_forward(ro, rd, geom, live, chan, vis, oracle.TraceConfig(), bvh=tree)
     assert fwd["nhit"].sum() > 1000
     _compare_forward(rt, fwd)
+
+
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7])
+def test_trace_variants_are_bit_identical(oracle, variant):
+    """Every forward-kernel variant (hit buffer size, register cap, packet shape) gives the same
+    bits as the oracle: the variant only changes speed."""
+    sc = synthetic.clustered_scene(40_000, seed=8)
+    chan = np.random.default_rng(2).uniform(0, 1, (sc.n, 3)).astype(np.float32)
+    W, H = 72, 56
+    rt = G.make_tracer(W, H, sc.mean, sc.rotation, sc.scale + np.float32(1.0), sc.opacity, channels=chan,
+                       t_threshold=0.001)
+    rt.set_trace_variant(variant)
+    cam = synthetic.orbit_camera(1.1, W, H, radius=4.0)
+    ro, rd = _camera_rays_gpu(rt, cam)
+    geom, l2w, aabb, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, sc.scale + np.float32(1.0), sc.opacity)
+    fwd = oracle.trace_forward(ro, rd, geom, live, chan, vis, oracle.TraceConfig(t_threshold=0.001),
+                               bvh=oracle.Bvh(aabb, vis))
+    assert fwd["nacc"].max() > 20  # more than one 16-key buffer on some rays
+    _compare_forward(rt, fwd)
