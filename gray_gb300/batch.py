@@ -83,7 +83,8 @@ class _Plan:
 
 class BatchRenderer:
     def __init__(self, tracers, use_graph: bool = True, autotune: bool = True, variant: int | None = None,
-                 blocks_per_sm: int | None = None, znear: float = 0.0, zfar: float = 99999.9):
+                 blocks_per_sm: int | None = None, znear: float = 0.0, zfar: float = 99999.9,
+                 cache_plans: bool = True):
         self.L = _bind()
         self.tracers = list(tracers)
         self.device = self.tracers[0].device
@@ -93,6 +94,7 @@ class BatchRenderer:
         self.znear, self.zfar = float(znear), float(zfar)
         self.status = torch.zeros(1, device=self.device, dtype=torch.int32)
         self.plans = {}
+        self.cache_plans = cache_plans or use_graph
         self.tuned = {}
         self._scenes_dev = None
         self._scene_ptrs = None
@@ -232,7 +234,8 @@ class BatchRenderer:
         if plan is None:
             variant, bps = self._tune(sreqs)
             plan = self._plan(sreqs, variant, bps)
-            self.plans[sig] = plan
+            if self.cache_plans:
+                self.plans[sig] = plan
             if self.use_graph:
                 self._launch(plan)  # warm-up outside capture
                 torch.cuda.synchronize(self.device)

@@ -170,11 +170,13 @@ class GaussianDataHolder:
                 t.resize_(n, 1)
                 if n > old:
                     t[old:] = first  # only element 0 is read; keep the rows consistent
-            for kind in ("grad_", "first_moment_", "second_moment_"):
-                for name in _PARAM_NAMES:
-                    self._resize(getattr(self, kind + name), self._shape(name, n), old)
-            for name in ("pruning_weight", "pruning_counter", "was_visible", "marked"):
-                self._resize(getattr(self, name), (n, 1), old)
+            if not self.inference_only:  # inference keeps one-row gradient/optimiser tensors (gaussians.h:226)
+                for kind in ("grad_", "first_moment_", "second_moment_"):
+                    for name in _PARAM_NAMES:
+                        self._resize(getattr(self, kind + name), self._shape(name, n), old)
+                for name in ("pruning_weight", "pruning_counter", "marked"):
+                    self._resize(getattr(self, name), (n, 1), old)
+            self._resize(self.was_visible, (n, 1), old)
         self._link_grads()
 
     @staticmethod
