@@ -146,6 +146,9 @@ struct f3 {
 };
 __device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
 __device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// a.b as an FMA chain: fma(a.z, b.z, fma(a.y, b.y, a.x * b.x))
+__device__ __forceinline__ float fdot3(f3 a, f3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
+__device__ __forceinline__ float fdot3(float4 a, f3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
 
 // Object-space ray of one Gaussian and its max-density point (reference: cuda/shaders.cu:17-49).
 // g0..g2 = rows (M | mu) of the snapshot.  With lo = M (o - mu) and ld = M d (d a unit world
@@ -161,16 +164,14 @@ struct LocalHit {
 __device__ __forceinline__ void local_ray(const float4 g0, const float4 g1, const float4 g2, f3 ro, f3 rd,
                                           LocalHit &h) {
     f3 rel = mk3(ro.x - g0.w, ro.y - g1.w, ro.z - g2.w);
-    h.lo = mk3(g0.x * rel.x + g0.y * rel.y + g0.z * rel.z, g1.x * rel.x + g1.y * rel.y + g1.z * rel.z,
-               g2.x * rel.x + g2.y * rel.y + g2.z * rel.z);
-    h.ld = mk3(g0.x * rd.x + g0.y * rd.y + g0.z * rd.z, g1.x * rd.x + g1.y * rd.y + g1.z * rd.z,
-               g2.x * rd.x + g2.y * rd.y + g2.z * rd.z);
-    h.b = dot3(h.lo, h.ld);
+    h.lo = mk3(fdot3(g0, rel), fdot3(g1, rel), fdot3(g2, rel));
+    h.ld = mk3(fdot3(g0, rd), fdot3(g1, rd), fdot3(g2, rd));
+    h.b = fdot3(h.lo, h.ld);
 }
 
 __device__ __forceinline__ void closest_point(LocalHit &h) {
-    h.t = -h.b / dot3(h.ld, h.ld);
-    h.u = mk3(h.lo.x + h.t * h.ld.x, h.lo.y + h.t * h.ld.y, h.lo.z + h.t * h.ld.z);
+    h.t = -h.b / fdot3(h.ld, h.ld);
+    h.u = mk3(fmaf(h.t, h.ld.x, h.lo.x), fmaf(h.t, h.ld.y, h.lo.y), fmaf(h.t, h.ld.z, h.lo.z));
 }
 
 // Segment [znear, zfar] of the object-space ray against the instance's unit box [-1, 1]^3 (the
@@ -199,14 +200,14 @@ __device__ __forceinline__ bool intersect(const float4 g0, const float4 g1, cons
     local_ray(g0, g1, g2, ro, rd, h);
     if (h.b > 0.0f) return false;
     closest_point(h);
-    float sq = dot3(h.u, h.u);
+    float sq = fdot3(h.u, h.u);
     if (sq > 1.0f) return false;
     dist = h.t;
     if (!(dist >= znear && dist <= zfar)) {
         if (!unit_box_overlap(h, znear, zfar)) return false;
     }
     f3 x = mk3(h.u.x * sf, h.u.y * sf, h.u.z * sf);
-    float gv = eval_gaussian(dot3(x, x), exp_power);
+    float gv = eval_gaussian(fdot3(x, x), exp_power);
     alpha = maxalpha_mul(gv, o);
     return true;
 }

@@ -30,6 +30,8 @@ constexpr int kMaxPasses = 99;               // MAX_ITERATIONS, cuda/forward_pas
 constexpr int kMaxTraversals = 4 * kMaxPasses * 2;  // bound on re-traversals of one ray
 constexpr int kDefaultTraceVariant = 1;
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kWideStack = 512;  // per-warp shared stack of the frustum traversal
+constexpr int kCand = 64;        // per-warp candidate leaves between flushes
 
 struct FwdArgs {
     uint32_t alloc_w, render_w, render_h;
@@ -58,15 +60,32 @@ __device__ __forceinline__ uint32_t pcg_hash(uint32_t v) {
     return (word >> 22u) ^ word;
 }
 
-__device__ __forceinline__ bool slab_hit(const float bmin[3], const float bmax[3], f3 ro, f3 inv, float eps) {
-    float ta = (bmin[0] - eps - ro.x) * inv.x, tb = (bmax[0] + eps - ro.x) * inv.x;
+// Ray against an axis-aligned box widened by the ray's rounding margin eps:
+// t = (b -/+ eps - o) * inv computed as fma(b, inv, c) with c_lo = -(o + eps) inv, c_hi = (eps - o) inv.
+struct SlabRay {
+    f3 inv, clo, chi;
+};
+
+__device__ __forceinline__ SlabRay make_slab_ray(f3 ro, f3 rd, float eps) {
+    SlabRay r;
+    float dx = fabsf(rd.x) < 1e-20f ? (rd.x < 0.0f ? -1e-20f : 1e-20f) : rd.x;
+    float dy = fabsf(rd.y) < 1e-20f ? (rd.y < 0.0f ? -1e-20f : 1e-20f) : rd.y;
+    float dz = fabsf(rd.z) < 1e-20f ? (rd.z < 0.0f ? -1e-20f : 1e-20f) : rd.z;
+    r.inv = mk3(1.0f / dx, 1.0f / dy, 1.0f / dz);
+    r.clo = mk3(-(ro.x + eps) * r.inv.x, -(ro.y + eps) * r.inv.y, -(ro.z + eps) * r.inv.z);
+    r.chi = mk3((eps - ro.x) * r.inv.x, (eps - ro.y) * r.inv.y, (eps - ro.z) * r.inv.z);
+    return r;
+}
+
+__device__ __forceinline__ bool slab_hit(const float bmin[3], const float bmax[3], const SlabRay &r) {
+    float ta = fmaf(bmin[0], r.inv.x, r.clo.x), tb = fmaf(bmax[0], r.inv.x, r.chi.x);
     float tn = fminf(ta, tb), tf = fmaxf(ta, tb);
-    ta = (bmin[1] - eps - ro.y) * inv.y;
-    tb = (bmax[1] + eps - ro.y) * inv.y;
+    ta = fmaf(bmin[1], r.inv.y, r.clo.y);
+    tb = fmaf(bmax[1], r.inv.y, r.chi.y);
     tn = fmaxf(tn, fminf(ta, tb));
     tf = fminf(tf, fmaxf(ta, tb));
-    ta = (bmin[2] - eps - ro.z) * inv.z;
-    tb = (bmax[2] + eps - ro.z) * inv.z;
+    ta = fmaf(bmin[2], r.inv.z, r.clo.z);
+    tb = fmaf(bmax[2], r.inv.z, r.chi.z);
     tn = fmaxf(tn, fminf(ta, tb));
     tf = fminf(tf, fmaxf(ta, tb));
     return tn <= tf && tf >= 0.0f;
@@ -169,13 +188,144 @@ __device__ __forceinline__ void stack_push(uint32_t &stk0, uint32_t &stk1, int &
     }
 }
 
+// Frustum of a packet of primary rays sharing one origin: four side planes through the origin and
+// the plane through the origin orthogonal to the packet's mean direction (nothing behind it can be
+// hit).  Normals point inside.  Stored per warp in shared memory.
+struct Frustum {
+    float o[3];
+    float n[5][3];
+};
+
+// Frustum of the rays through the pixels [x0, x1] x [y0, y1] of a pinhole camera: the rays of the
+// corner pixels span a convex cone that contains every ray of the rectangle.
+__device__ __forceinline__ void make_frustum(Frustum &fr, f3 o, const f3 d[4]) {
+    fr.o[0] = o.x;
+    fr.o[1] = o.y;
+    fr.o[2] = o.z;
+    const f3 c = mk3(d[0].x + d[1].x + d[2].x + d[3].x, d[0].y + d[1].y + d[2].y + d[3].y,
+                     d[0].z + d[1].z + d[2].z + d[3].z);
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const f3 a = d[e], b = d[(e + 1) & 3];
+        f3 nn = mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+        if (dot3(nn, c) < 0.0f) nn = mk3(-nn.x, -nn.y, -nn.z);
+        fr.n[e][0] = nn.x;
+        fr.n[e][1] = nn.y;
+        fr.n[e][2] = nn.z;
+    }
+    fr.n[4][0] = c.x;
+    fr.n[4][1] = c.y;
+    fr.n[4][2] = c.z;
+}
+
+// Conservative box-frustum test: false only when the box lies entirely outside one plane by more
+// than a rounding margin.
+__device__ __forceinline__ bool frustum_box(const Frustum &fr, const float bmin[3], const float bmax[3]) {
+#pragma unroll
+    for (int p = 0; p < 5; p++) {
+        const float nx = fr.n[p][0], ny = fr.n[p][1], nz = fr.n[p][2];
+        const float vx = (nx >= 0.0f ? bmax[0] : bmin[0]) - fr.o[0];
+        const float vy = (ny >= 0.0f ? bmax[1] : bmin[1]) - fr.o[1];
+        const float vz = (nz >= 0.0f ? bmax[2] : bmin[2]) - fr.o[2];
+        const float sdist = fmaf(nz, vz, fmaf(ny, vy, nx * vx));
+        const float margin = 1e-5f * (fabsf(nx) + fabsf(ny) + fabsf(nz)) * (fabsf(vx) + fabsf(vy) + fabsf(vz)) + 1e-30f;
+        if (sdist < -margin) return false;
+    }
+    return true;
+}
+
+// One full traversal of the packet (camera rays with a common origin) with the node work spread
+// over the lanes: each step pops up to 32 nodes, one per lane, tests their child boxes against the
+// packet frustum, pushes surviving internal children and queues surviving leaves; queued leaves
+// are then intersected by every lane with its own ray (on_leaf).  Returns false if the shared
+// stack overflowed (the caller then repeats the traversal per ray).
+template <int KB>
+__device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool want,
+                                                 bool first, LaneState &st, unsigned long long (*kbuf)[kFwdThreads],
+                                                 const Frustum &fr, uint32_t *stk, uint32_t *cand,
+                                                 int32_t *status) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lanemask_lt = (1u << lane) - 1u;
+    const int n = sc.n;
+    const float *rb = sc.root_box;
+    const float rmin[3] = {rb[0], rb[1], rb[2]}, rmax[3] = {rb[4], rb[5], rb[6]};
+    if (n <= 0 || !frustum_box(fr, rmin, rmax)) return true;
+    if (n == 1) {
+        on_leaf<KB>(sc, 0u, want, first, ro, rd, k, st, kbuf);
+        return true;
+    }
+    if (lane == 0) stk[0] = 0u;
+    __syncwarp();
+    int sp = 1, nc = 0;
+    bool ok = true;
+    long long budget = (long long)n;  // a valid tree pushes each internal node at most once per traversal
+    while (sp > 0) {
+        if (--budget < 0) {
+            raise_status(status, GRAY_STATUS_STACK_OVERFLOW);
+            break;
+        }
+        const int take = sp < 32 ? sp : 32;
+        uint32_t node = GRAY_NULL;
+        if (lane < take) node = stk[sp - 1 - lane];
+        __syncwarp();
+        sp -= take;
+        bool p0 = false, p1 = false;
+        uint32_t c0 = 0, c1 = 0;
+        if (node != GRAY_NULL) {
+            if (node >= (uint32_t)(n - 1)) {
+                raise_status(status, GRAY_STATUS_STACK_OVERFLOW);
+            } else {
+                const float4 q0 = sc.nodes[4 * node], q1 = sc.nodes[4 * node + 1], q2 = sc.nodes[4 * node + 2],
+                             q3 = sc.nodes[4 * node + 3];
+                const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
+                const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
+                c0 = __float_as_uint(q3.x);
+                c1 = __float_as_uint(q3.y);
+                p0 = frustum_box(fr, b0min, b0max);
+                p1 = frustum_box(fr, b1min, b1max);
+            }
+        }
+        const bool i0 = p0 && !(c0 & GRAY_LEAF_BIT), i1 = p1 && !(c1 & GRAY_LEAF_BIT);
+        const bool l0 = p0 && (c0 & GRAY_LEAF_BIT) && (c0 & ~GRAY_LEAF_BIT) < (uint32_t)n;
+        const bool l1 = p1 && (c1 & GRAY_LEAF_BIT) && (c1 & ~GRAY_LEAF_BIT) < (uint32_t)n;
+        const uint32_t m0 = __ballot_sync(kFull, i0), m1 = __ballot_sync(kFull, i1);
+        const int n0 = __popc(m0), n1 = __popc(m1);
+        if (sp + n0 + n1 > kWideStack) {
+            ok = false;  // frontier too wide for the shared stack
+            break;
+        }
+        if (i0) stk[sp + __popc(m0 & lanemask_lt)] = c0;
+        if (i1) stk[sp + n0 + __popc(m1 & lanemask_lt)] = c1;
+        sp += n0 + n1;
+        const uint32_t q0m = __ballot_sync(kFull, l0), q1m = __ballot_sync(kFull, l1);
+        const int lq0 = __popc(q0m), lq1 = __popc(q1m);
+        if (nc + lq0 + lq1 > kCand) {
+            __syncwarp();
+            for (int j = 0; j < nc; j++) on_leaf<KB>(sc, cand[j], want, first, ro, rd, k, st, kbuf);
+            __syncwarp();
+            nc = 0;
+        }
+        if (l0) cand[nc + __popc(q0m & lanemask_lt)] = c0 & ~GRAY_LEAF_BIT;
+        if (l1) cand[nc + lq0 + __popc(q1m & lanemask_lt)] = c1 & ~GRAY_LEAF_BIT;
+        nc += lq0 + lq1;
+        __syncwarp();
+    }
+    if (ok) {
+        for (int j = 0; j < nc; j++) on_leaf<KB>(sc, cand[j], want, first, ro, rd, k, st, kbuf);
+    }
+    __syncwarp();
+    return ok;
+}
+
 // Trace the warp's 32 rays (one per lane; `alive` lanes only) through the scene: traversal,
 // selection, compositing (cuda/forward_pass.cu:6-151 minus the write-out).  Every lane of the
 // warp must call this together.
 template <int KB>
 __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool alive,
                                           bool grads, const HitSink &hs, int32_t *status,
-                                          unsigned long long (*kbuf)[kFwdThreads], RayResult &res) {
+                                          unsigned long long (*kbuf)[kFwdThreads], RayResult &res,
+                                          const Frustum *fr = nullptr, uint32_t *wstk = nullptr,
+                                          uint32_t *wcand = nullptr) {
     const int lane = threadIdx.x & 31;
     LaneState &st = res.st;
     st.ft = 1.0f;
@@ -192,14 +342,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
     bool done = !alive;
     uint32_t head = GRAY_NULL;
 
-    f3 inv;
-    {
-        float dx = fabsf(rd.x) < 1e-20f ? (rd.x < 0.0f ? -1e-20f : 1e-20f) : rd.x;
-        float dy = fabsf(rd.y) < 1e-20f ? (rd.y < 0.0f ? -1e-20f : 1e-20f) : rd.y;
-        float dz = fabsf(rd.z) < 1e-20f ? (rd.z < 0.0f ? -1e-20f : 1e-20f) : rd.z;
-        inv = mk3(1.0f / dx, 1.0f / dy, 1.0f / dz);
-    }
-    const float eps = 2.0e-6f * (fabsf(ro.x) + fabsf(ro.y) + fabsf(ro.z));
+    const SlabRay sr = make_slab_ray(ro, rd, 2.0e-6f * (fabsf(ro.x) + fabsf(ro.y) + fabsf(ro.z)));
     // packet lead direction for the near/far child order (any deterministic choice is valid)
     float lx = alive ? rd.x : 0.0f, ly = alive ? rd.y : 0.0f, lz = alive ? rd.z : 0.0f;
 #pragma unroll
@@ -217,10 +360,23 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
         st.kcount = 0;
         st.ncand = 0;
         // ---------------- traversal ----------------
-        if (n == 1) {
+        bool per_ray = fr == nullptr;
+        if (!per_ray && !traverse_frustum<KB>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, status)) {
+            // the frustum traversal gave up (stack overflow): discard what it gathered, trace per ray
+            st.kcount = 0;
+            st.ncand = 0;
+            if (first) {
+                st.ft = 1.0f;
+                st.afx = st.cfx0 = st.cfx1 = st.cfx2 = 0;
+                st.nhit = 0;
+            }
+            per_ray = true;
+        }
+        if (!per_ray) {
+        } else if (n == 1) {
             const float *rb = sc.root_box;
             const float bmin[3] = {rb[0], rb[1], rb[2]}, bmax[3] = {rb[4], rb[5], rb[6]};
-            bool h = want && slab_hit(bmin, bmax, ro, inv, eps);
+            bool h = want && slab_hit(bmin, bmax, sr);
             if (__any_sync(kFull, h)) on_leaf<KB>(sc, 0u, h, first, ro, rd, k, st, kbuf);
         } else if (n > 1) {
             uint32_t stk0 = 0, stk1 = 0;  // entry e lives in lane e%32, word e/32
@@ -228,13 +384,18 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
             {
                 const float *rb = sc.root_box;
                 const float bmin[3] = {rb[0], rb[1], rb[2]}, bmax[3] = {rb[4], rb[5], rb[6]};
-                bool h = want && slab_hit(bmin, bmax, ro, inv, eps);
+                bool h = want && slab_hit(bmin, bmax, sr);
                 if (__any_sync(kFull, h)) {
                     if (lane == 0) stk0 = 0u;
                     sp = 1;
                 }
             }
+            long long budget = 2LL * n;  // pops of a valid tree per traversal are < n
             while (sp > 0) {
+                if (--budget < 0) {
+                    raise_status(status, GRAY_STATUS_STACK_OVERFLOW);
+                    break;
+                }
                 sp--;
                 const uint32_t word = (sp >> 5) == 0 ? stk0 : stk1;
                 const uint32_t node = __shfl_sync(kFull, word, sp & 31);
@@ -247,8 +408,8 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
                 const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
                 const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
                 const uint32_t c0 = __float_as_uint(q3.x), c1 = __float_as_uint(q3.y);
-                const bool h0 = want && slab_hit(b0min, b0max, ro, inv, eps);
-                const bool h1 = want && slab_hit(b1min, b1max, ro, inv, eps);
+                const bool h0 = want && slab_hit(b0min, b0max, sr);
+                const bool h1 = want && slab_hit(b1min, b1max, sr);
                 const bool any0 = __any_sync(kFull, h0), any1 = __any_sync(kFull, h1);
                 if (!any0 && !any1) continue;
                 // near child first along the packet's lead direction
@@ -421,6 +582,9 @@ __device__ __forceinline__ f3 camera_ray(const float *w, float fov, int px, int 
 template <int KB, int MINB>
 __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const FwdArgs a) {
     __shared__ unsigned long long kbuf[KB][kFwdThreads];
+    __shared__ Frustum sfr[kWarps];
+    __shared__ uint32_t sstk[kWarps][kWideStack];
+    __shared__ uint32_t scand[kWarps][kCand];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int px = blockIdx.x * (a.tile_w * kBlockWarpsX) + (warp % kBlockWarpsX) * a.tile_w + (lane % a.tile_w);
     const int py = blockIdx.y * (a.tile_h * kBlockWarpsY) + (warp / kBlockWarpsX) * a.tile_h + (lane / a.tile_w);
@@ -458,8 +622,24 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const 
         alive = !(sqrtf(dot3(rd, rd)) == 0.0f);
     }
 
+    // camera rays of the packet share the origin: trace with the frustum traversal
+    const bool frustum = !*a.rays_from_python && !*a.jitter;
+    if (frustum) {
+        const int x0 = px - lane % a.tile_w, y0 = py - lane / a.tile_w;
+        const int x1 = x0 + a.tile_w - 1, y1 = y0 + a.tile_h - 1;
+        if (lane == 0) {
+            const f3 o = mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]);
+            const f3 d[4] = {camera_ray(a.w2c, *a.fov, x0, y0, a.render_w, a.render_h, 0.0f, 0.0f),
+                             camera_ray(a.w2c, *a.fov, x1, y0, a.render_w, a.render_h, 0.0f, 0.0f),
+                             camera_ray(a.w2c, *a.fov, x1, y1, a.render_w, a.render_h, 0.0f, 0.0f),
+                             camera_ray(a.w2c, *a.fov, x0, y1, a.render_w, a.render_h, 0.0f, 0.0f)};
+            make_frustum(sfr[warp], o, d);
+        }
+        __syncwarp();
+    }
     RayResult r;
-    trace_ray<KB>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r);
+    trace_ray<KB>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sstk[warp],
+                  scand[warp]);
 
     if (!inside) return;
     if (!alive) {
@@ -510,9 +690,13 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
                        int nviews, uint32_t total_packets, float *__restrict__ out, uint32_t *__restrict__ counter,
                        int tile_w, int32_t *status) {
     __shared__ unsigned long long kbuf[KB][kFwdThreads];
-    const int lane = threadIdx.x & 31;
+    __shared__ Frustum sfr[kWarps];
+    __shared__ uint32_t sstk[kWarps][kWideStack];
+    __shared__ uint32_t scand[kWarps][kCand];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tile_h = 32 / tile_w;
     for (;;) {
+        __syncwarp();
         uint32_t packet = 0;
         if (lane == 0) packet = atomicAdd(counter, 1u);
         packet = __shfl_sync(kFull, packet, 0);
@@ -539,8 +723,18 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
         f3 ro = mk3(vw.origin[0], vw.origin[1], vw.origin[2]);
         f3 rd = mk3(0.0f, 0.0f, 0.0f);
         if (inside) rd = camera_ray(vw.w2c, vw.fov_y, px, py, vw.width, vw.height, 0.0f, 0.0f);
+        if (lane == 0) {
+            const int x0 = (int)((local % tiles_x) * tile_w), y0 = (int)((local / tiles_x) * tile_h);
+            const int x1 = x0 + tile_w - 1, y1 = y0 + tile_h - 1;
+            const f3 d[4] = {camera_ray(vw.w2c, vw.fov_y, x0, y0, vw.width, vw.height, 0.0f, 0.0f),
+                             camera_ray(vw.w2c, vw.fov_y, x1, y0, vw.width, vw.height, 0.0f, 0.0f),
+                             camera_ray(vw.w2c, vw.fov_y, x1, y1, vw.width, vw.height, 0.0f, 0.0f),
+                             camera_ray(vw.w2c, vw.fov_y, x0, y1, vw.width, vw.height, 0.0f, 0.0f)};
+            make_frustum(sfr[warp], ro, d);
+        }
+        __syncwarp();
         RayResult r;
-        trace_ray<KB>(sc, k, ro, rd, inside, false, hs, status, kbuf, r);
+        trace_ray<KB>(sc, k, ro, rd, inside, false, hs, status, kbuf, r, &sfr[warp], sstk[warp], scand[warp]);
         if (!inside) continue;
         float r0, r1, r2;
         finish_ray(r, bs.bg, 1e-12f, false, r0, r1, r2);
@@ -695,7 +889,7 @@ __global__ void __launch_bounds__(128) trace_backward_kernel(const BwdArgs a) {
             local_ray(g0, g1, g2, ro, rd, h);
             closest_point(h);
             const f3 x = mk3(h.u.x * sf, h.u.y * sf, h.u.z * sf);
-            const float sq = dot3(x, x);
+            const float sq = fdot3(x, x);
             const float gv = eval_gaussian(sq, pw);
             const float alpha = maxalpha_mul(gv, o);
 

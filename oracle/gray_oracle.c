@@ -594,6 +594,9 @@ typedef struct {
     float dist, alpha;
 } is_result;
 
+/* a.b as an FMA chain: fma(a2, b2, fma(a1, b1, a0 * b0)) (the GPU kernels use the same chain) */
+static inline float fdot3(const float *a, const float *b) { return fmaf(a[2], b[2], fmaf(a[1], b[1], a[0] * b[0])); }
+
 /* cuda/shaders.cu:10-67.  g = 12-float snapshot row block, o/sf live. */
 static inline is_result intersect(const float *g, float o, float sf, const float ro[3], const float rd[3],
                                   const orc_trace_cfg *cfg) {
@@ -603,15 +606,15 @@ static inline is_result intersect(const float *g, float o, float sf, const float
     float lo[3], ld[3];
     for (int r = 0; r < 3; r++) {
         const float *m = g + 4 * r;
-        lo[r] = m[0] * rel[0] + m[1] * rel[1] + m[2] * rel[2];
-        ld[r] = m[0] * rd[0] + m[1] * rd[1] + m[2] * rd[2];
+        lo[r] = fdot3(m, rel);
+        ld[r] = fdot3(m, rd);
     }
     /* world distance of the max-density point: t = -<lo,ld>/<ld,ld> (d is a unit vector) */
-    float b = lo[0] * ld[0] + lo[1] * ld[1] + lo[2] * ld[2];
+    float b = fdot3(lo, ld);
     if (b > 0.0f) return res;
-    float t = -b / (ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
-    float u[3] = {lo[0] + t * ld[0], lo[1] + t * ld[1], lo[2] + t * ld[2]};
-    float sq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    float t = -b / fdot3(ld, ld);
+    float u[3] = {fmaf(t, ld[0], lo[0]), fmaf(t, ld[1], lo[1]), fmaf(t, ld[2], lo[2])};
+    float sq = fdot3(u, u);
     if (sq > 1.0f) return res;
     float dist = t;
     if (!(dist >= cfg->znear && dist <= cfg->zfar)) {
@@ -627,7 +630,7 @@ static inline is_result intersect(const float *g, float o, float sf, const float
         if (!(t0 <= t1)) return res;
     }
     float x[3] = {u[0] * sf, u[1] * sf, u[2] * sf};
-    float d = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+    float d = fdot3(x, x);
     float gv = eval_gaussian(d, cfg->exp_power);
     res.hit = 1;
     res.dist = dist;
@@ -926,14 +929,14 @@ static void backward_range(const bwd_job *J) {
             float lo[3], ld[3];
             for (int k = 0; k < 3; k++) {
                 const float *m = g + 4 * k;
-                lo[k] = m[0] * rel[0] + m[1] * rel[1] + m[2] * rel[2];
-                ld[k] = m[0] * rd[0] + m[1] * rd[1] + m[2] * rd[2];
+                lo[k] = fdot3(m, rel);
+                ld[k] = fdot3(m, rd);
             }
-            float b = lo[0] * ld[0] + lo[1] * ld[1] + lo[2] * ld[2];
-            float td = -b / (ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
+            float b = fdot3(lo, ld);
+            float td = -b / fdot3(ld, ld);
             float x[3];
-            for (int k = 0; k < 3; k++) x[k] = (lo[k] + td * ld[k]) * sf;
-            float sq = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+            for (int k = 0; k < 3; k++) x[k] = fmaf(td, ld[k], lo[k]) * sf;
+            float sq = fdot3(x, x);
             float gv = eval_gaussian(sq, cfg->exp_power);
             float alpha = orc_maxalpha_mul(gv, o);
 
