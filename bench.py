@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-stride", type=int, default=24, help="1 ray in stride^2 pixels for the CPU sample")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and served measurements")
+    ap.add_argument("--serve-requests", type=int, default=2000)
     return ap.parse_args()
 
 
@@ -253,6 +255,9 @@ def gpu_arm(a, rank, world, local_rank):
                 "shares": {k: round(v[0] / total_ms, 4) for k, v in sorted(res.items(), key=lambda kv: -kv[1][0])},
                 "hits_per_ray": round(H / R, 2), "composited_per_ray": round(A / R, 2)}
 
+    batched = None if a.no_extras else batched_form(a, rt.cuda_module)
+    served = None if a.no_extras else served_form(a, rank)
+
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
         cpu = cpu_baseline(a, sc, cam)
@@ -264,8 +269,113 @@ def gpu_arm(a, rank, world, local_rank):
             "rays_per_s": round(rays_per_s, 1), "train_rays_per_s": round(R * steps_per_s, 1),
             "e2e": {"value": round(e2e_steps_per_s, 3), "unit": "train-steps/s",
                     "h2d_bytes_per_step": int(target_host.numel() * 4), "d2h_bytes_per_step": 4},
-            "gpu_launches": launches, "roofline": roofline, "clocks": clk, "cpu_baseline": cpu}
+            "gpu_launches": launches, "roofline": roofline, "clocks": clk, "cpu_baseline": cpu,
+            "batched": batched, "served": served}
     return line
+
+
+def batched_form(a, tracer):
+    """16 views of uneven resolution ({640x480, 1280x720, 1600x1040, 1920x1080}, radius-8 orbit, +-15
+    degree jitter) of the benchmark scene: one persistent launch replayed from a CUDA graph with an
+    autotuned kernel variant, against 16 plain one-view launches (forward_pass_display)."""
+    import torch
+
+    from gray_gb300 import synthetic
+    from gray_gb300.batch import BatchRenderer
+
+    cams = synthetic.uneven_cameras(16, seed=0)
+    rays = sum(c.image_width * c.image_height for c in cams)
+
+    def plain():
+        for c in cams:
+            t = tracer.get_camera()
+            t.znear.fill_(0.0)
+            t.zfar.fill_(99999.9)
+            t.vertical_fov_radians.fill_(float(c.fov_y))
+            t.set_pose(c.origin_cuda(), c.rotation_c2w_blender_cuda())
+            tracer.get_config().rays_from_python.fill_(False)
+            tracer.set_render_resolution(c.image_width, c.image_height)
+            with torch.no_grad():
+                tracer.forward_pass_display()
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms_plain = timed(plain, 3)
+    br = BatchRenderer([tracer], use_graph=True, autotune=True)
+    reqs = [(0, c) for c in cams]
+    ms_batch = timed(lambda: br.render(reqs), 5)
+    tracer.set_render_resolution(a.width, a.height)
+    return {"views": 16, "rays": rays, "plain_ms": round(ms_plain, 3), "batched_ms": round(ms_batch, 3),
+            "plain_rays_per_s": round(rays / ms_plain * 1000.0, 1),
+            "batched_rays_per_s": round(rays / ms_batch * 1000.0, 1),
+            "speedup": round(ms_plain / ms_batch, 3), "tuned": [list(v) for v in br.tuned.values()]}
+
+
+def served_form(a, rank):
+    """Four resident inference scenes (0.5M, 1M, 3M, 6M clustered Gaussians, different seeds, fp16 SH);
+    Poisson arrivals at 200 req/s, each naming a scene, a random orbit pose and a resolution uniform in
+    {640x480, 1280x720, 1920x1080, 3840x2160}; continuous batching vs the plain one-request-per-launch
+    loop on the same schedule."""
+    import numpy as np
+    import torch
+
+    from gray_gb300 import classes, synthetic
+    from gray_gb300.serve import RenderServer, plain_loop, poisson_arrivals, run_served
+
+    sizes = [500_000, 1_000_000, 3_000_000, 6_000_000]
+    tracers = []
+    for i, n in enumerate(sizes):
+        sc = synthetic.clustered_scene(n, seed=100 + i)
+        t = classes.Raytracer(3840, 2160, n, 3, 1, 1, inference_only=True)
+        t.get_config().t_threshold.fill_(0.03)
+        g = t.get_gaussians()
+        with torch.no_grad():
+            for k, v in (("mean", sc.mean), ("rotation", sc.rotation), ("scale", sc.scale),
+                         ("opacity", sc.opacity), ("sh_coeffs_dc", sc.sh_dc), ("sh_coeffs_rest", sc.sh_rest)):
+                getattr(g, k).copy_(torch.from_numpy(v))
+            g.current_sh_degree.fill_(3)
+        t.rebuild_bvh()
+        tracers.append(t)
+        del sc
+    rng = np.random.default_rng(7 + rank)
+    res = [(640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
+    count = a.serve_requests
+    sched = []
+    for t_arr in poisson_arrivals(200.0, count, seed=3 + rank):
+        w, h = res[int(rng.integers(0, 4))]
+        sched.append((float(t_arr), int(rng.integers(0, 4)),
+                      synthetic.orbit_camera(float(rng.uniform(0, 2 * np.pi)), w, h,
+                                             jitter_rad=tuple(rng.uniform(-0.26, 0.26, 2)))))
+    # warm-up (autotune-free eager launches; first-touch allocations)
+    warm = RenderServer(tracers, slots=2, max_batch=16)
+    for s_, cam in [(i, synthetic.orbit_camera(0.1, 640, 480)) for i in range(4)]:
+        warm.submit(s_, cam)
+    warm.drain()
+    torch.cuda.synchronize()
+    srv = RenderServer(tracers, slots=2, max_batch=16)
+    reqs, wall = run_served(srv, sched)
+    lat = np.array([r.latency for r in reqs]) * 1000.0
+    rays = sum(r.rays for r in reqs)
+    plain, wall_p = plain_loop(tracers, sched)
+    lat_p = np.array([l for l, _ in plain]) * 1000.0
+    out = {"requests": count, "rate_hz": 200.0, "scenes": sizes,
+           "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
+           "rays_per_s": round(rays / wall, 1),
+           "plain_p50_ms": round(float(np.percentile(lat_p, 50)), 2),
+           "plain_p99_ms": round(float(np.percentile(lat_p, 99)), 2),
+           "plain_rays_per_s": round(rays / wall_p, 1), "offered_rays_per_s": round(rays / sched[-1][0], 1)}
+    del tracers
+    torch.cuda.empty_cache()
+    return out
 
 
 # ----------------------------------------------------------------------------------------------

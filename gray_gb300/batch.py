@@ -58,6 +58,8 @@ def _check(L, rc, what):
         raise _lib.GrayError(f"{what}: {L.gray_last_error().decode()} (code {rc})")
 
 
+# untuned choice: 4x8 packets with a 16-entry k-buffer (the library's default variant), 8 blocks per SM
+DEFAULT_VARIANT, DEFAULT_BLOCKS_PER_SM = 7, 8
 # candidates the autotuner tries: (kernel variant, persistent blocks per SM)
 TUNE_CANDIDATES = [(v, b) for v in (1, 2, 3, 5, 7) for b in (4, 6, 8)]
 
@@ -90,7 +92,7 @@ class BatchRenderer:
         self.device = self.tracers[0].device
         self.use_graph = use_graph
         self.autotune = autotune and variant is None
-        self.fixed = (variant or 1, blocks_per_sm or 4)
+        self.fixed = (variant or DEFAULT_VARIANT, blocks_per_sm or DEFAULT_BLOCKS_PER_SM)
         self.znear, self.zfar = float(znear), float(zfar)
         self.status = torch.zeros(1, device=self.device, dtype=torch.int32)
         self.plans = {}

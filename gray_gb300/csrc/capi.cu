@@ -213,7 +213,7 @@ int gray_rebuild_bvh(const gray_params *p, void *stream) {
 }
 
 uint32_t gray_batch_packets(uint32_t width, uint32_t height, int32_t variant) {
-    const int v = variant > 0 ? variant : 1;
+    const int v = variant > 0 ? variant : gray::kDefaultTraceVariant;
     const uint32_t tw = (v & 4) ? 4u : 8u, th = 32u / tw;
     return ((width + tw - 1) / tw) * ((height + th - 1) / th);
 }

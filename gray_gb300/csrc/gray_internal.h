@@ -8,6 +8,10 @@
 
 namespace gray {
 
+// forward-kernel variant used when gray_params.trace_variant (or a batch launch's variant) is 0:
+// 4x8 packets, 16-entry k-buffer, 8 blocks per SM
+constexpr int kDefaultTraceVariant = 7;
+
 // scene.cu
 cudaError_t launch_snapshot(const gray_params &p, cudaStream_t s);
 // reset_frame: zero was_visible, count the call and empty the backward hit list (forward_pass)

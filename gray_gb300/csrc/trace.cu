@@ -28,7 +28,6 @@ constexpr int kStackMax = 32 * kStackWords;
 constexpr int kPassSlots = 32;               // BUFFER_SIZE, cuda/forward_pass.cu:4
 constexpr int kMaxPasses = 99;               // MAX_ITERATIONS, cuda/forward_pass.cu:3
 constexpr int kMaxTraversals = 4 * kMaxPasses * 2;  // bound on re-traversals of one ray
-constexpr int kDefaultTraceVariant = 1;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWideStack = 512;  // per-warp shared stack of the frustum traversal
 constexpr int kCand = 64;        // per-warp candidate leaves between flushes

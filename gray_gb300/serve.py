@@ -24,7 +24,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
-from .batch import BatchRenderer
+from .batch import DEFAULT_BLOCKS_PER_SM, DEFAULT_VARIANT, BatchRenderer
 from .camera import CameraInfo
 
 
@@ -58,12 +58,13 @@ class _Slot:
 
 class RenderServer:
     def __init__(self, tracers, slots: int = 2, max_batch: int = 32, reserve_bytes: int = 4 << 30,
-                 keep_images: bool = False, variant: int | None = None):
+                 keep_images: bool = False, variant: int | None = None, blocks_per_sm: int | None = None):
         self.tracers = list(tracers)
         self.device = self.tracers[0].device
         self.slots = [_Slot(torch.cuda.Stream(self.device),
-                            BatchRenderer(self.tracers, use_graph=False, autotune=False, variant=variant or 1,
-                                          blocks_per_sm=4, cache_plans=False)) for _ in range(slots)]
+                            BatchRenderer(self.tracers, use_graph=False, autotune=False,
+                                          variant=variant or DEFAULT_VARIANT,
+                                          blocks_per_sm=blocks_per_sm or DEFAULT_BLOCKS_PER_SM, cache_plans=False)) for _ in range(slots)]
         self.max_batch = max_batch
         self.reserve = reserve_bytes
         self.keep_images = keep_images
