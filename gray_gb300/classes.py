@@ -458,7 +458,9 @@ class Raytracer:
             self.status.zero_()
             raise _lib.GrayError(f"device status {v:#x}: " + ", ".join(
                 n for bit, n in ((1, "backward hit list overflow (increase ppll_backward_size)"),
-                                 (2, "BVH traversal limit exceeded"), (4, "refit budget exhausted")) if v & bit))
+                                 (2, "BVH traversal limit exceeded"), (4, "refit budget exhausted"),
+                                 (8, "render_ellipsoids=True is only supported for no-grad display renders"))
+                if v & bit))
 
     def scene_workspace(self):
         return self._scene

@@ -155,6 +155,7 @@ int gray_forward_pass(const gray_params *p, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     GRAY_LAUNCH("forward_prep", gray::launch_forward_prep(*p, true, s));
     GRAY_LAUNCH("trace_forward", gray::launch_trace_forward(*p, s));
+    GRAY_LAUNCH("ellipsoids", gray::launch_ellipsoids(*p, s));
     return GRAY_OK;
 }
 
@@ -164,6 +165,7 @@ int gray_forward_pass_display(const gray_params *p, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     GRAY_LAUNCH("forward_prep", gray::launch_forward_prep(*p, false, s));
     GRAY_LAUNCH("trace_forward", gray::launch_trace_forward(*p, s));
+    GRAY_LAUNCH("ellipsoids", gray::launch_ellipsoids(*p, s));
     return GRAY_OK;
 }
 

@@ -39,6 +39,8 @@ struct FwdArgs {
     const float *cam_origin, *fov, *w2c, *znear, *zfar;
     const float *exp_power, *alpha_threshold, *t_threshold, *eps_fwd, *bg;
     const uint8_t *render_depth, *needs_ray_output, *rays_from_python, *jitter, *grads_enabled;
+    const uint8_t *render_ellipsoids;
+    const float *ellipsoid_min_opacity;
     const uint32_t *total_num_calls;
     const float4 *geom;
     const float2 *live;
@@ -584,6 +586,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const 
     __shared__ Frustum sfr[kWarps];
     __shared__ uint32_t sstk[kWarps][kWideStack];
     __shared__ uint32_t scand[kWarps][kCand];
+    if (*a.render_ellipsoids) return;  // the ellipsoid view (ellipsoid_kernel) renders this frame
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int px = blockIdx.x * (a.tile_w * kBlockWarpsX) + (warp % kBlockWarpsX) * a.tile_w + (lane % a.tile_w);
     const int py = blockIdx.y * (a.tile_h * kBlockWarpsY) + (warp / kBlockWarpsX) * a.tile_h + (lane / a.tile_w);
@@ -679,6 +682,179 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const 
 }
 
 // ---------------------------------------------------------------------------------------------
+// Ellipsoid view (reference: cuda/ellipsoid_viewer.cu:1-94): closest-hit ray tracing of each
+// Gaussian's support ellipsoid (the unit sphere of its snapshot frame), flat-shaded.  A Gaussian
+// takes part if its snapshot marked it visible and its live opacity is >= ellipsoid_min_opacity.
+// Per Gaussian the hit distance is the near root t0 = (s - h) / |ld| of the object-space ray when
+// t0 >= znear, else the far root t1 = (s + h) / |ld|; the ray keeps the smallest distance in
+// [znear, zfar] (equal distances: the smaller gaussian id, where OptiX keeps whichever its
+// traversal reported first).  Output: RGB = max(0.5, <-view, normal>) (colour + 0.15) and depth =
+// t, or the background and depth 0 on a miss; an inactive pixel (zero direction) is left as is.
+// ---------------------------------------------------------------------------------------------
+constexpr int kEllStack = 64;
+
+// Distance of the ray's hit on Gaussian gid's ellipsoid, if it has one at or beyond tmin.
+__device__ __forceinline__ bool ellipsoid_hit(const float4 g0, const float4 g1, const float4 g2, f3 ro, f3 rd,
+                                              float tmin, float &t) {
+    LocalHit h;
+    local_ray(g0, g1, g2, ro, rd, h);
+    if (h.b > 0.0f) return false;  // centre behind the ray
+    const float norm = sqrtf(fdot3(h.ld, h.ld));
+    const f3 dn = mk3(h.ld.x / norm, h.ld.y / norm, h.ld.z / norm);
+    const float smid = -fdot3(h.lo, dn);
+    const f3 u = mk3(fmaf(smid, dn.x, h.lo.x), fmaf(smid, dn.y, h.lo.y), fmaf(smid, dn.z, h.lo.z));
+    const float sq = fdot3(u, u);
+    if (sq > 1.0f) return false;
+    const float hc = sqrtf(1.0f - sq);
+    const float t0 = (smid - hc) / norm, t1 = (smid + hc) / norm;
+    t = t0 >= tmin ? t0 : t1;
+    return t >= tmin;
+}
+
+// Flat shading of the winning hit: object-space normal at the hit, carried to world space by the
+// transpose of the snapshot matrix M (the inverse-transpose of the instance transform).
+__device__ __forceinline__ void ellipsoid_shade(const float4 g0, const float4 g1, const float4 g2, f3 ro, f3 rd,
+                                                float t, const float *c, float &r0, float &r1, float &r2) {
+    LocalHit h;
+    local_ray(g0, g1, g2, ro, rd, h);
+    const float norm = sqrtf(fdot3(h.ld, h.ld));
+    const f3 dn = mk3(h.ld.x / norm, h.ld.y / norm, h.ld.z / norm);
+    const float tn = t * norm;
+    f3 ln = mk3(fmaf(tn, dn.x, h.lo.x), fmaf(tn, dn.y, h.lo.y), fmaf(tn, dn.z, h.lo.z));
+    const float ll = sqrtf(fdot3(ln, ln));
+    ln = mk3(ln.x / ll, ln.y / ll, ln.z / ll);
+    f3 wn = mk3(fmaf(ln.z, g2.x, fmaf(ln.y, g1.x, ln.x * g0.x)), fmaf(ln.z, g2.y, fmaf(ln.y, g1.y, ln.x * g0.y)),
+                fmaf(ln.z, g2.z, fmaf(ln.y, g1.z, ln.x * g0.z)));
+    const float wl = sqrtf(fdot3(wn, wn));
+    wn = mk3(wn.x / wl, wn.y / wl, wn.z / wl);
+    const float dl = sqrtf(fdot3(rd, rd));
+    const f3 vd = mk3(rd.x / dl, rd.y / dl, rd.z / dl);
+    const float align = fmaxf(0.5f, -fdot3(vd, wn));
+    r0 = align * (c[0] + 0.15f);
+    r1 = align * (c[1] + 0.15f);
+    r2 = align * (c[2] + 0.15f);
+}
+
+// Entry distance of the ray into a box (slab test of SlabRay), or false if it misses.
+__device__ __forceinline__ bool slab_enter(const float bmin[3], const float bmax[3], const SlabRay &r, float &tn) {
+    float ta = fmaf(bmin[0], r.inv.x, r.clo.x), tb = fmaf(bmax[0], r.inv.x, r.chi.x);
+    float n0 = fminf(ta, tb), f0 = fmaxf(ta, tb);
+    ta = fmaf(bmin[1], r.inv.y, r.clo.y);
+    tb = fmaf(bmax[1], r.inv.y, r.chi.y);
+    n0 = fmaxf(n0, fminf(ta, tb));
+    f0 = fminf(f0, fmaxf(ta, tb));
+    ta = fmaf(bmin[2], r.inv.z, r.clo.z);
+    tb = fmaf(bmax[2], r.inv.z, r.chi.z);
+    n0 = fmaxf(n0, fminf(ta, tb));
+    f0 = fminf(f0, fmaxf(ta, tb));
+    tn = n0;
+    return n0 <= f0 && f0 >= 0.0f;
+}
+
+__device__ __forceinline__ void ellipsoid_leaf(const FwdArgs &a, uint32_t gid, f3 ro, f3 rd, float znear, float minop,
+                                               float &best, uint32_t &bid) {
+    if (a.live[gid].x < minop) return;
+    float t;
+    if (!ellipsoid_hit(a.geom[3 * gid], a.geom[3 * gid + 1], a.geom[3 * gid + 2], ro, rd, znear, t)) return;
+    if (t < best || (t == best && gid < bid)) {
+        best = t;
+        bid = gid;
+    }
+}
+
+constexpr int kEllTileX = 16, kEllTileY = 8;
+
+__global__ void __launch_bounds__(kEllTileX * kEllTileY) ellipsoid_kernel(const FwdArgs a) {
+    if (!*a.render_ellipsoids) return;
+    const int px = blockIdx.x * kEllTileX + threadIdx.x, py = blockIdx.y * kEllTileY + threadIdx.y;
+    if (px >= (int)a.render_w || py >= (int)a.render_h) return;
+    const uint32_t pixel = (uint32_t)py * a.alloc_w + (uint32_t)px;
+    if (*a.grads_enabled) raise_status(a.status, GRAY_STATUS_BAD_MODE);
+    f3 ro, rd;
+    if (*a.rays_from_python) {
+        ro = mk3(a.ray_o[3 * pixel], a.ray_o[3 * pixel + 1], a.ray_o[3 * pixel + 2]);
+        rd = mk3(a.ray_d[3 * pixel], a.ray_d[3 * pixel + 1], a.ray_d[3 * pixel + 2]);
+    } else {
+        ro = mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]);
+        float jx = 0.0f, jy = 0.0f;
+        if (*a.jitter) {
+            uint32_t h = pcg_hash(pixel ^ pcg_hash(*a.total_num_calls));
+            jx = (float)(h & 0xFFFFu) * 0x1.0p-16f - 0.5f;
+            jy = (float)(h >> 16) * 0x1.0p-16f - 0.5f;
+        }
+        rd = camera_ray(a.w2c, *a.fov, px, py, a.render_w, a.render_h, jx, jy);
+    }
+    a.head[pixel] = GRAY_NULL;  // no backward hit list for this frame
+    if (sqrtf(dot3(rd, rd)) == 0.0f) return;
+    const float znear = *a.znear, minop = *a.ellipsoid_min_opacity;
+    float best = *a.zfar;
+    uint32_t bid = GRAY_NULL;
+    const int n = a.n;
+    const SlabRay sr = make_slab_ray(ro, rd, 2.0e-6f * (fabsf(ro.x) + fabsf(ro.y) + fabsf(ro.z)));
+    if (n == 1) {
+        ellipsoid_leaf(a, 0u, ro, rd, znear, minop, best, bid);
+    } else if (n > 1) {
+        uint32_t stk[kEllStack];
+        int sp = 0;
+        float tr;
+        const float *rb = a.root_box;
+        const float rmin[3] = {rb[0], rb[1], rb[2]}, rmax[3] = {rb[4], rb[5], rb[6]};
+        if (slab_enter(rmin, rmax, sr, tr) && tr <= best) stk[sp++] = 0u;
+        long long budget = 2LL * n;
+        while (sp > 0) {
+            if (--budget < 0) {
+                raise_status(a.status, GRAY_STATUS_STACK_OVERFLOW);
+                break;
+            }
+            const uint32_t node = stk[--sp];
+            if (node >= (uint32_t)(n - 1)) {
+                raise_status(a.status, GRAY_STATUS_STACK_OVERFLOW);
+                continue;
+            }
+            const float4 q0 = a.nodes[4 * node], q1 = a.nodes[4 * node + 1], q2 = a.nodes[4 * node + 2],
+                         q3 = a.nodes[4 * node + 3];
+            const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
+            const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
+            const uint32_t c0 = __float_as_uint(q3.x), c1 = __float_as_uint(q3.y);
+            float t0, t1;
+            bool h0 = slab_enter(b0min, b0max, sr, t0) && t0 <= best;
+            bool h1 = slab_enter(b1min, b1max, sr, t1) && t1 <= best;
+            // leaves right away (they may shrink `best` before the boxes are pushed)
+            if (h0 && (c0 & GRAY_LEAF_BIT)) {
+                if ((c0 & ~GRAY_LEAF_BIT) < (uint32_t)n) ellipsoid_leaf(a, c0 & ~GRAY_LEAF_BIT, ro, rd, znear, minop, best, bid);
+                h0 = false;
+            }
+            if (h1 && (c1 & GRAY_LEAF_BIT)) {
+                if ((c1 & ~GRAY_LEAF_BIT) < (uint32_t)n) ellipsoid_leaf(a, c1 & ~GRAY_LEAF_BIT, ro, rd, znear, minop, best, bid);
+                h1 = false;
+            }
+            h0 = h0 && t0 <= best;
+            h1 = h1 && t1 <= best;
+            // far child deeper in the stack, near child on top
+            const bool near1 = h0 && h1 && t1 < t0;
+            const uint32_t first = near1 ? c0 : c1, second = near1 ? c1 : c0;
+            const bool hf = near1 ? h0 : h1, hs = near1 ? h1 : h0;
+            if (sp + (int)hf + (int)hs > kEllStack) {
+                raise_status(a.status, GRAY_STATUS_STACK_OVERFLOW);
+                break;
+            }
+            if (hf) stk[sp++] = first;
+            if (hs) stk[sp++] = second;
+        }
+    }
+    float r0 = a.bg[0], r1 = a.bg[1], r2 = a.bg[2], depth = 0.0f;
+    if (bid != GRAY_NULL) {
+        ellipsoid_shade(a.geom[3 * bid], a.geom[3 * bid + 1], a.geom[3 * bid + 2], ro, rd, best,
+                        a.channels + 3 * (size_t)bid, r0, r1, r2);
+        depth = best;
+    }
+    a.out_rgb[3 * pixel] = r0;
+    a.out_rgb[3 * pixel + 1] = r1;
+    a.out_rgb[3 * pixel + 2] = r2;
+    a.out_depth[pixel] = depth;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Batched render: many views (of one or several resident scenes) in one persistent launch.
 // Warps pull 32-ray packets from a global counter; packet -> (view, tile) through the views'
 // packet offsets.  Forward only (no gradients, no hit lists); per view the output is RGB.
@@ -744,7 +920,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
     }
 }
 
-cudaError_t launch_trace_forward(const gray_params &p, cudaStream_t s) {
+static FwdArgs forward_args(const gray_params &p) {
     FwdArgs a;
     a.alloc_w = p.image_width;
     a.render_w = p.render_width;
@@ -785,6 +961,22 @@ cudaError_t launch_trace_forward(const gray_params &p, cudaStream_t s) {
     a.pool = p.hitlist.pool;
     a.pool_size = p.hitlist.size;
     a.status = p.status;
+    a.render_ellipsoids = p.config.render_ellipsoids;
+    a.ellipsoid_min_opacity = p.config.ellipsoid_min_opacity;
+    a.tile_w = 8;
+    a.tile_h = 4;
+    return a;
+}
+
+cudaError_t launch_ellipsoids(const gray_params &p, cudaStream_t s) {
+    const FwdArgs a = forward_args(p);
+    dim3 grid((p.render_width + kEllTileX - 1) / kEllTileX, (p.render_height + kEllTileY - 1) / kEllTileY);
+    ellipsoid_kernel<<<grid, dim3(kEllTileX, kEllTileY), 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_forward(const gray_params &p, cudaStream_t s) {
+    FwdArgs a = forward_args(p);
     // variant: bits 0-1 select (buffer size, register cap), bit 2 the packet shape
     const int v = p.trace_variant > 0 ? p.trace_variant : kDefaultTraceVariant;
     a.tile_w = (v & 4) ? 4 : 8;

@@ -42,6 +42,8 @@ extern "C" {
 #define GRAY_STATUS_HITLIST_OVERFLOW 1    /* backward hit list full (reference: PPLL overflow __trap) */
 #define GRAY_STATUS_STACK_OVERFLOW 2      /* BVH traversal stack exhausted */
 #define GRAY_STATUS_REFIT_TIMEOUT 4       /* bottom-up refit spin budget exhausted */
+#define GRAY_STATUS_BAD_MODE 8            /* render_ellipsoids set on a forward with gradients enabled
+                                             (reference: assertion, gray/raytracer.py:142-144) */
 
 /* Gaussian parameters and optimiser state (cuda/core/gaussians.h:7-65). */
 typedef struct gray_gaussians {

@@ -1096,3 +1096,123 @@ void orc_adam_step(orc_adam_state *s, int step, int zero_grads, int update_chann
         }
     }
 }
+
+/* ------------------------------------------------------------------------------------------ */
+/* ellipsoid view: cuda/ellipsoid_viewer.cu:1-94 (closest hit on each Gaussian's support        */
+/* ellipsoid, flat shading).  Brute force over all Gaussians: the winner (smallest distance in  */
+/* [znear, zfar], equal distances -> smaller id) does not depend on visiting order.            */
+/* ------------------------------------------------------------------------------------------ */
+static void local_ray3(const float *g, const float ro[3], const float rd[3], float lo[3], float ld[3]) {
+    float rel[3] = {ro[0] - g[3], ro[1] - g[7], ro[2] - g[11]};
+    for (int r = 0; r < 3; r++) {
+        lo[r] = fdot3(g + 4 * r, rel);
+        ld[r] = fdot3(g + 4 * r, rd);
+    }
+}
+
+/* cuda/ellipsoid_viewer.cu:23-62: near root if at or beyond tmin, else far root */
+static int ellipsoid_hit(const float *g, const float ro[3], const float rd[3], float tmin, float *t) {
+    float lo[3], ld[3];
+    local_ray3(g, ro, rd, lo, ld);
+    if (fdot3(lo, ld) > 0.0f) return 0;
+    float norm = sqrtf(fdot3(ld, ld));
+    float dn[3] = {ld[0] / norm, ld[1] / norm, ld[2] / norm};
+    float smid = -fdot3(lo, dn);
+    float u[3] = {fmaf(smid, dn[0], lo[0]), fmaf(smid, dn[1], lo[1]), fmaf(smid, dn[2], lo[2])};
+    float sq = fdot3(u, u);
+    if (sq > 1.0f) return 0;
+    float hc = sqrtf(1.0f - sq);
+    float t0 = (smid - hc) / norm, t1 = (smid + hc) / norm;
+    *t = t0 >= tmin ? t0 : t1;
+    return *t >= tmin;
+}
+
+/* cuda/ellipsoid_viewer.cu:55-59, 66-93: world normal = M^T (object normal), flat shading */
+static void ellipsoid_shade(const float *g, const float ro[3], const float rd[3], float t, const float *c,
+                            float *rgb) {
+    float lo[3], ld[3];
+    local_ray3(g, ro, rd, lo, ld);
+    float norm = sqrtf(fdot3(ld, ld));
+    float dn[3] = {ld[0] / norm, ld[1] / norm, ld[2] / norm};
+    float tn = t * norm;
+    float ln[3] = {fmaf(tn, dn[0], lo[0]), fmaf(tn, dn[1], lo[1]), fmaf(tn, dn[2], lo[2])};
+    float ll = sqrtf(fdot3(ln, ln));
+    for (int k = 0; k < 3; k++) ln[k] = ln[k] / ll;
+    float wn[3];
+    for (int k = 0; k < 3; k++) wn[k] = fmaf(ln[2], g[8 + k], fmaf(ln[1], g[4 + k], ln[0] * g[k]));
+    float wl = sqrtf(fdot3(wn, wn));
+    for (int k = 0; k < 3; k++) wn[k] = wn[k] / wl;
+    float dl = sqrtf(fdot3(rd, rd));
+    float vd[3] = {rd[0] / dl, rd[1] / dl, rd[2] / dl};
+    float align = fmaxf(0.5f, -fdot3(vd, wn));
+    for (int k = 0; k < 3; k++) rgb[k] = align * (c[k] + 0.15f);
+}
+
+typedef struct {
+    int nrays;
+    const float *ray_o, *ray_d;
+    int n;
+    const float *geom, *live, *channels;
+    float znear, zfar, min_opacity;
+    const float *bg;
+    float *out_rgb, *out_depth;
+    int32_t *out_id;
+    int next;
+    pthread_mutex_t mu;
+} ell_job;
+
+static void *ell_worker(void *arg) {
+    ell_job *J = (ell_job *)arg;
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        int r0 = J->next;
+        J->next += 64;
+        pthread_mutex_unlock(&J->mu);
+        if (r0 >= J->nrays) break;
+        int r1 = r0 + 64 < J->nrays ? r0 + 64 : J->nrays;
+        for (int r = r0; r < r1; r++) {
+            const float *ro = J->ray_o + 3 * (size_t)r, *rd = J->ray_d + 3 * (size_t)r;
+            float *rgb = J->out_rgb + 3 * (size_t)r;
+            if (sqrtf(rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2]) == 0.0f) {
+                J->out_id[r] = -2; /* inactive pixel: outputs untouched */
+                continue;
+            }
+            float best = J->zfar;
+            int64_t bid = -1;
+            for (int i = 0; i < J->n; i++) {
+                if (J->live[2 * (size_t)i] < J->min_opacity) continue;
+                float t;
+                if (!ellipsoid_hit(J->geom + 12 * (size_t)i, ro, rd, J->znear, &t)) continue;
+                if (t < best || (t == best && bid < 0)) {
+                    best = t;
+                    bid = i;
+                }
+            }
+            J->out_id[r] = (int32_t)bid;
+            if (bid < 0) {
+                for (int k = 0; k < 3; k++) rgb[k] = J->bg[k];
+                J->out_depth[r] = 0.0f;
+            } else {
+                ellipsoid_shade(J->geom + 12 * (size_t)bid, ro, rd, best, J->channels + 3 * (size_t)bid, rgb);
+                J->out_depth[r] = best;
+            }
+        }
+    }
+    return NULL;
+}
+
+void orc_ellipsoids(int nrays, const float *ray_o, const float *ray_d, int n, const float *geom, const float *live,
+                    const float *channels, float znear, float zfar, float min_opacity, const float *bg,
+                    float *out_rgb, float *out_depth, int32_t *out_id, int nthreads) {
+    ell_job J = {nrays, ray_o, ray_d, n, geom, live, channels, znear, zfar, min_opacity, bg, out_rgb, out_depth,
+                 out_id, 0, PTHREAD_MUTEX_INITIALIZER};
+    if (nthreads <= 0) nthreads = orc_hardware_threads();
+    if (nthreads == 1) {
+        ell_worker(&J);
+        return;
+    }
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    for (int t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, ell_worker, &J);
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    free(th);
+}

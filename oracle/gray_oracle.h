@@ -120,6 +120,13 @@ typedef struct {
 void orc_adam_step(orc_adam_state *s, int step, int zero_grads, int update_channels, float beta1, float beta2,
                    float eps, int enable_sh, int sh_update_laziness);
 
+/* ---- ellipsoid view (cuda/ellipsoid_viewer.cu:1-94) ----
+ * live = [n,2] (opacity or -inf if invisible, sf); out_id = winning gaussian, -1 miss, -2 inactive
+ * ray (outputs untouched). */
+void orc_ellipsoids(int nrays, const float *ray_o, const float *ray_d, int n, const float *geom, const float *live,
+                    const float *channels, float znear, float zfar, float min_opacity, const float *bg,
+                    float *out_rgb, float *out_depth, int32_t *out_id, int nthreads);
+
 int orc_hardware_threads(void);
 
 #ifdef __cplusplus

@@ -95,6 +95,8 @@ def lib():
             ctypes.c_int, ctypes.c_int, ctypes.c_int, F32P, F32P, F32P, F32P, F32P, F32P, I64P, U32P,
             ctypes.c_int, F32P, F32P, F32P, F32P, F32P, F32P, ctypes.POINTER(_TraceCfg), ctypes.c_float, F64P,
             ctypes.c_int]
+        L.orc_ellipsoids.argtypes = [ctypes.c_int, F32P, F32P, ctypes.c_int, F32P, F32P, F32P, ctypes.c_float,
+                                     ctypes.c_float, ctypes.c_float, F32P, F32P, F32P, I32P, ctypes.c_int]
         L.orc_hardware_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -139,6 +141,10 @@ def expf(x: float) -> float:
 
 def logf(x: float) -> float:
     return lib().orc_logf(x)
+
+
+def scaling_factor(opacity: float, alpha_threshold=0.01, exp_power=2.0) -> float:
+    return float(lib().orc_scaling_factor(opacity, alpha_threshold, exp_power))
 
 
 def snapshot(mean, rotation, scale, opacity, alpha_threshold=0.01, exp_power=2.0, global_scale_factor=1.0):
@@ -271,6 +277,20 @@ def trace_backward(launch_w, launch_h, ray_o, ray_d, fwd, grad_out, geom, l2w, o
         _f32(l2w), _f32(opacity).reshape(-1), _f32(scale), _f32(rotation), _f32(channels), ctypes.byref(cfg.c()),
         eps_scale_grad, grad, nthreads)
     return grad
+
+
+def ellipsoids(ray_o, ray_d, geom, live, channels, znear=0.0, zfar=99999.9, min_opacity=0.0, bg=(0.0, 0.0, 0.0),
+               nthreads=0):
+    """Ellipsoid view (cuda/ellipsoid_viewer.cu:1-94), brute force.  Returns rgb [R,3], depth [R]
+    and the winning gaussian per ray (-1 miss, -2 inactive ray whose outputs stay as given: zeros)."""
+    ray_o, ray_d, geom, live, channels = map(_f32, (ray_o, ray_d, geom, live, channels))
+    R = ray_o.shape[0]
+    rgb = np.zeros((R, 3), np.float32)
+    depth = np.zeros(R, np.float32)
+    ids = np.zeros(R, np.int32)
+    lib().orc_ellipsoids(R, ray_o, ray_d, geom.shape[0], geom, live, channels, znear, zfar, min_opacity,
+                         _f32(np.asarray(bg, np.float32)), rgb, depth, ids, nthreads)
+    return rgb, depth, ids
 
 
 def hardware_threads() -> int:
