@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--cpu-sample-stride", type=int, default=24, help="1 ray in stride^2 pixels for the CPU sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and served measurements")
     ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--no-served", action="store_true", help="skip the served measurement only")
     return ap.parse_args()
 
 
@@ -256,7 +257,7 @@ def gpu_arm(a, rank, world, local_rank):
                 "hits_per_ray": round(H / R, 2), "composited_per_ray": round(A / R, 2)}
 
     batched = None if a.no_extras else batched_form(a, rt.cuda_module)
-    served = None if a.no_extras else served_form(a, rank)
+    served = None if (a.no_extras or a.no_served) else served_form(a, rank)
 
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:

@@ -5,8 +5,10 @@ torch.classes.gray.Raytracer and `gray_gb300.Raytracer` mirrors gray.raytracer.R
 run hand-written CUDA kernels from libgray_gb300.so (built by `python -m gray_gb300.build`).
 """
 from . import classes
-from .camera import CameraInfo, look_at
+from .cadence import TrainCadence
+from .camera import CameraInfo, load_cameras_json, look_at, save_cameras_json
 from .config import RaytracerConfig
 from .raytracer import Raytracer
 
-__all__ = ["CameraInfo", "RaytracerConfig", "Raytracer", "classes", "look_at"]
+__all__ = ["CameraInfo", "RaytracerConfig", "Raytracer", "TrainCadence", "classes", "load_cameras_json", "look_at",
+           "save_cameras_json"]

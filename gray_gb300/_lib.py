@@ -63,7 +63,7 @@ class HitlistC(ctypes.Structure):
 
 class SceneC(ctypes.Structure):
     _fields_ = _ptrs("geom", "l2w", "aabb", "visible", "live", "grad_acc", "nodes", "int_parent", "leaf_parent",
-                     "order", "codes", "refit_flags", "sort_tmp", "root_box", "bounds") + [
+                     "order", "codes", "refit_flags", "sort_tmp", "root_box", "bounds", "bwd_rec") + [
         ("bvh_valid", ctypes.c_int32)]
 
 

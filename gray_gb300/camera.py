@@ -83,3 +83,31 @@ def look_at(origin, target=(0.0, 0.0, 0.0), up=(0.0, 0.0, 1.0), fov_y=0.8, width
     fov_x = 2.0 * math.atan(math.tan(fov_y / 2.0) * width / height)
     return CameraInfo(uid=uid, R=R, T=-R.T @ o, origin=o, fov_y=fov_y, fov_x=fov_x, image_width=width,
                       image_height=height)
+
+
+def save_cameras_json(model_path: str, cameras) -> str:
+    """Write `cameras` as the scene's cameras.json: a list of CameraInfo.to_json() records (the file
+    gray/scene.py:156-170 and render.py read back)."""
+    import json
+    import os
+
+    path = os.path.join(model_path, "cameras.json")
+    with open(path, "w") as f:
+        json.dump([c.to_json() for c in cameras], f)
+    return path
+
+
+def load_cameras_json(model_path: str):
+    """gray/scene.py:156-170 without the images: cameras.json next to `model_path` (a directory, or
+    a file inside it), sorted by image_name and split into (train, test) by is_test."""
+    import json
+    import os
+
+    model_dir = os.path.dirname(model_path) if os.path.isfile(model_path) else model_path
+    path = os.path.join(model_dir, "cameras.json")
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"No colmap dataset and no cameras.json found at '{path}'")
+    with open(path) as f:
+        payload = json.load(f)
+    cams = sorted((CameraInfo.from_json(e) for e in payload), key=lambda c: c.image_name)
+    return [c for c in cams if not c.is_test], [c for c in cams if c.is_test]

@@ -270,7 +270,7 @@ class PPLLDataHolder:
 class _SceneWorkspace:
     """Device buffers of the instance snapshot and the LBVH for n Gaussians."""
 
-    def __init__(self, n: int, device):
+    def __init__(self, n: int, device, training: bool = True):
         n = max(int(n), 0)
         m = max(n - 1, 1)
         nn = max(n, 1)
@@ -293,12 +293,13 @@ class _SceneWorkspace:
         self.sort_tmp = torch.zeros(max(words, 1), **i32)
         self.root_box = torch.zeros(8, **f)
         self.bounds = torch.zeros(8, **i32)
+        self.bwd_rec = torch.zeros(nn if training else 1, 24, **f)
         self.bvh_valid = False
 
     def struct(self) -> _lib.SceneC:
         s = _lib.SceneC()
         for name in ("geom", "l2w", "aabb", "visible", "live", "grad_acc", "nodes", "int_parent", "leaf_parent",
-                     "order", "codes", "refit_flags", "sort_tmp", "root_box", "bounds"):
+                     "order", "codes", "refit_flags", "sort_tmp", "root_box", "bounds", "bwd_rec"):
             setattr(s, name, _p(getattr(self, name)))
         s.bvh_valid = int(self.bvh_valid)
         return s
@@ -328,7 +329,7 @@ class Raytracer:
                                                  1 if inference_only else ppll_backward_size, dev)
         self.status = torch.zeros(1, device=dev, dtype=torch.int32)
         self.trace_variant = 0  # forward-kernel variant (0 = library default); results do not depend on it
-        self._scene = _SceneWorkspace(1, dev)
+        self._scene = _SceneWorkspace(1, dev, not self.inference_only)
         self._params = None
         if num_gaussians > 0:
             self.resize(num_gaussians)
@@ -402,7 +403,7 @@ class Raytracer:
 
     def resize(self, new_num_gaussians: int):
         self.gaussian_data.resize(new_num_gaussians)
-        self._scene = _SceneWorkspace(self.gaussian_data.count, self.device)
+        self._scene = _SceneWorkspace(self.gaussian_data.count, self.device, not self.inference_only)
         self._invalidate()
 
     def set_trace_variant(self, variant: int):

@@ -154,8 +154,8 @@ int gray_forward_pass(const gray_params *p, void *stream) {
     if (e) return e;
     cudaStream_t s = (cudaStream_t)stream;
     GRAY_LAUNCH("forward_prep", gray::launch_forward_prep(*p, true, s));
-    GRAY_LAUNCH("trace_forward", gray::launch_trace_forward(*p, s));
-    GRAY_LAUNCH("ellipsoids", gray::launch_ellipsoids(*p, s));
+    GRAY_LAUNCH("trace_forward", gray::launch_trace_forward(*p, false, s));
+    GRAY_LAUNCH("ellipsoids", gray::launch_ellipsoids(*p, false, s));
     return GRAY_OK;
 }
 
@@ -164,8 +164,8 @@ int gray_forward_pass_display(const gray_params *p, void *stream) {
     if (e) return e;
     cudaStream_t s = (cudaStream_t)stream;
     GRAY_LAUNCH("forward_prep", gray::launch_forward_prep(*p, false, s));
-    GRAY_LAUNCH("trace_forward", gray::launch_trace_forward(*p, s));
-    GRAY_LAUNCH("ellipsoids", gray::launch_ellipsoids(*p, s));
+    GRAY_LAUNCH("trace_forward", gray::launch_trace_forward(*p, true, s));
+    GRAY_LAUNCH("ellipsoids", gray::launch_ellipsoids(*p, true, s));
     return GRAY_OK;
 }
 
@@ -173,7 +173,7 @@ int gray_backward_pass(const gray_params *p, void *stream) {
     int e = check_trace(p);
     if (e) return e;
     if (p->gaussians.sh_is_fp16) return fail(GRAY_ERR_INVALID_ARGUMENT, "backward_pass needs an inference_only=False raytracer");
-    if (!p->scene.grad_acc || !p->gaussians.grad_mean)
+    if (!p->scene.grad_acc || !p->scene.bwd_rec || !p->gaussians.grad_mean)
         return fail(GRAY_ERR_INVALID_ARGUMENT, "missing gradient buffers");
     cudaStream_t s = (cudaStream_t)stream;
     GRAY_LAUNCH("trace_backward", gray::launch_trace_backward(*p, s));

@@ -212,6 +212,16 @@ __device__ __forceinline__ bool intersect(const float4 g0, const float4 g1, cons
     return true;
 }
 
+// Full transmittance prod(1 - alpha) over all hits of a ray, kept order-independent: the sum of
+// log(1 - alpha) in 2^-40 fixed point, exponentiated once at the end.  Terms are <= 0; once the sum
+// is below -105 (exp underflows to 0 in fp32) further terms are not added, which bounds it for any
+// number of hits.
+constexpr long long kLogFixFloor = -105LL * (1LL << 40);
+__device__ __forceinline__ void add_log_transmittance(long long &s, float alpha) {
+    if (s > kLogFixFloor) s += to_fixed(glog(1.0f - alpha), 0x1.0p40f);
+}
+__device__ __forceinline__ float full_transmittance(long long s) { return gexp(__ll2float_rn(s) * 0x1.0p-40f); }
+
 // alpha * 2^24 for an fp16 alpha in [0, 1): an exact integer, from the half's bits
 __device__ __forceinline__ long long alpha16_fixed(uint16_t a16) {
     const uint32_t e = (a16 >> 10) & 0x1fu, m = a16 & 0x3ffu;

@@ -26,9 +26,10 @@ cudaError_t launch_lbvh_refit(const gray_params &p, cudaStream_t s);
 size_t sort_tmp_words(int n);
 
 // trace.cu
-cudaError_t launch_trace_forward(const gray_params &p, cudaStream_t s);
+// display: forward_pass_display (colour only; no hit lists or saved state, whatever grads_enabled holds)
+cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_t s);
 // ellipsoid view; a no-op launch unless config.render_ellipsoids is set
-cudaError_t launch_ellipsoids(const gray_params &p, cudaStream_t s);
+cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s);
 cudaError_t launch_trace_backward(const gray_params &p, cudaStream_t s);
 cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int nviews,
                                uint32_t total_packets, float *out, uint32_t *counter, int variant, int blocks_per_sm,

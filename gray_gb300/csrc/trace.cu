@@ -41,6 +41,7 @@ struct FwdArgs {
     const uint8_t *render_depth, *needs_ray_output, *rays_from_python, *jitter, *grads_enabled;
     const uint8_t *render_ellipsoids;
     const float *ellipsoid_min_opacity;
+    int display;  // forward_pass_display: colour only, whatever grads_enabled holds
     const uint32_t *total_num_calls;
     const float4 *geom;
     const float2 *live;
@@ -93,7 +94,8 @@ __device__ __forceinline__ bool slab_hit(const float bmin[3], const float bmax[3
 }
 
 struct LaneState {
-    // all-hit accumulators (first traversal only)
+    // all-hit accumulators (first traversal only); ft is set from lfx when the ray finishes
+    long long lfx;
     float ft;
     long long afx, cfx0, cfx1, cfx2;
     int nhit;
@@ -143,7 +145,7 @@ __device__ __forceinline__ void on_leaf(const TraceScene &sc, uint32_t gid, bool
     if (!intersect(g0, g1, g2, lv.x, lv.y, ro, rd, k.athr, k.pw, k.znear, k.zfar, dist, alpha)) return;
     const uint16_t a16 = f2h_bits(alpha), d16 = f2h_bits(dist);
     if (first) {
-        st.ft = fmaf(-st.ft, alpha, st.ft);
+        add_log_transmittance(st.lfx, alpha);
         const float af = h2f_bits(a16);
         const float *c = sc.channels + 3 * (size_t)gid;
         st.afx += alpha16_fixed(a16);
@@ -329,7 +331,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
                                           uint32_t *wcand = nullptr) {
     const int lane = threadIdx.x & 31;
     LaneState &st = res.st;
-    st.ft = 1.0f;
+    st.lfx = 0;
     st.afx = st.cfx0 = st.cfx1 = st.cfx2 = 0;
     st.nhit = 0;
     st.kcount = 0;
@@ -367,7 +369,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
             st.kcount = 0;
             st.ncand = 0;
             if (first) {
-                st.ft = 1.0f;
+                st.lfx = 0;
                 st.afx = st.cfx0 = st.cfx1 = st.cfx2 = 0;
                 st.nhit = 0;
             }
@@ -541,6 +543,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
     res.C0 = C0;
     res.C1 = C1;
     res.C2 = C2;
+    st.ft = full_transmittance(st.lfx);
     res.depth = depth;
     res.nacc = nacc;
     res.head = head;
@@ -600,7 +603,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const 
     k.pw = *a.exp_power;
     k.tthr = *a.t_threshold;
     k.render_depth = *a.render_depth != 0;
-    const bool grads = *a.grads_enabled != 0;
+    const bool grads = !a.display && *a.grads_enabled != 0;
     const TraceScene sc{a.geom, a.live, a.channels, a.nodes, a.root_box, a.n};
     const HitSink hs{a.counter, a.pool, a.pool_size};
 
@@ -769,7 +772,7 @@ __global__ void __launch_bounds__(kEllTileX * kEllTileY) ellipsoid_kernel(const 
     const int px = blockIdx.x * kEllTileX + threadIdx.x, py = blockIdx.y * kEllTileY + threadIdx.y;
     if (px >= (int)a.render_w || py >= (int)a.render_h) return;
     const uint32_t pixel = (uint32_t)py * a.alloc_w + (uint32_t)px;
-    if (*a.grads_enabled) raise_status(a.status, GRAY_STATUS_BAD_MODE);
+    if (!a.display && *a.grads_enabled) raise_status(a.status, GRAY_STATUS_BAD_MODE);
     f3 ro, rd;
     if (*a.rays_from_python) {
         ro = mk3(a.ray_o[3 * pixel], a.ray_o[3 * pixel + 1], a.ray_o[3 * pixel + 2]);
@@ -920,8 +923,9 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
     }
 }
 
-static FwdArgs forward_args(const gray_params &p) {
+static FwdArgs forward_args(const gray_params &p, bool display) {
     FwdArgs a;
+    a.display = display ? 1 : 0;
     a.alloc_w = p.image_width;
     a.render_w = p.render_width;
     a.render_h = p.render_height;
@@ -968,15 +972,15 @@ static FwdArgs forward_args(const gray_params &p) {
     return a;
 }
 
-cudaError_t launch_ellipsoids(const gray_params &p, cudaStream_t s) {
-    const FwdArgs a = forward_args(p);
+cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s) {
+    const FwdArgs a = forward_args(p, display);
     dim3 grid((p.render_width + kEllTileX - 1) / kEllTileX, (p.render_height + kEllTileY - 1) / kEllTileY);
     ellipsoid_kernel<<<grid, dim3(kEllTileX, kEllTileY), 0, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_trace_forward(const gray_params &p, cudaStream_t s) {
-    FwdArgs a = forward_args(p);
+cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_t s) {
+    FwdArgs a = forward_args(p, display);
     // variant: bits 0-1 select (buffer size, register cap), bit 2 the packet shape
     const int v = p.trace_variant > 0 ? p.trace_variant : kDefaultTraceVariant;
     a.tile_w = (v & 4) ? 4 : 8;
@@ -1019,10 +1023,7 @@ struct BwdArgs {
     uint32_t alloc_w, render_w, render_h;
     int n;
     const float *exp_power, *alpha_threshold, *eps_scale_grad, *bg;
-    const float4 *geom, *l2w;
-    const float2 *live;
-    const float *scale, *channels;
-    const float4 *rotation;
+    const float4 *geom, *rec;
     const float *pix_T, *pix_fullT, *pix_rem, *ray_o, *ray_d, *grad_out;
     const uint32_t *head, *pool;
     uint32_t pool_size;
@@ -1031,127 +1032,257 @@ struct BwdArgs {
 };
 
 __device__ __forceinline__ void red_add4(float *addr, float x, float y, float z, float w) {
-    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(x), "f"(y), "f"(z), "f"(w)
-                 : "memory");
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(x), "f"(y), "f"(z), "f"(w));
 }
 
+// Adds one hit's 16 gradient values to the Gaussian's accumulator row.  Neighbouring pixels
+// composite the same Gaussians at the same replay step, and vector reductions on one row serialise
+// in L2, so the lanes of the warp that hold the same Gaussian first combine their values with
+// shuffles and the lowest of them issues the four reductions.
+__device__ __forceinline__ void reduce_hit(float *row, uint32_t gid, float (&v)[16]) {
+    const unsigned active = __activemask();
+    const unsigned grp = __match_any_sync(active, gid);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(grp) - 1;
+    unsigned rest = grp & ~(1u << leader);
+    while (rest) {
+        const int src = __ffs(rest) - 1;
+        rest &= rest - 1;
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            const float t = __shfl_sync(grp, v[k], src);
+            if (lane == leader) v[k] += t;
+        }
+    }
+    if (lane == leader) {
+        red_add4(row, v[0], v[1], v[2], v[3]);
+        red_add4(row + 4, v[4], v[5], v[6], v[7]);
+        red_add4(row + 8, v[8], v[9], v[10], v[11]);
+        red_add4(row + 12, v[12], v[13], v[14], v[15]);
+    }
+}
+
+// Per-Gaussian backward record: what the reverse replay needs of one Gaussian besides its snapshot
+// rows (M | mu), precomputed once per backward pass instead of once per composited hit.  Written
+// from the state the forward used: live opacity o and scaling factor sf, colour c, current log-scale
+// and rotation q, snapshot L2W rows L.  24 floats (6 x float4):
+//   [o, sf, 1/|q|, s0] [s1, s2, c0, c1] [c2, K00, K01, K02] [K10, K11, K12, K20] [K21, K22, 0, 0]
+//   [qn0, qn1, qn2, qn3]
+// with s = exp(scale), K_rk = L_rk / (s_k sf + eps_scale_grad) * s_k (the scale gradient's factor,
+// cuda/backward_pass.cu:101-111) and qn = q / |q|.
+constexpr int kRecVec = 6;
+
+__global__ void __launch_bounds__(256) bwd_record_kernel(int n, const float2 *__restrict__ live,
+                                                         const float *__restrict__ scale,
+                                                         const float4 *__restrict__ rotation,
+                                                         const float *__restrict__ channels,
+                                                         const float4 *__restrict__ l2w,
+                                                         const float *__restrict__ eps_scale_grad,
+                                                         float4 *__restrict__ rec) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 lv = live[i];
+    const float sf = lv.y, eps = *eps_scale_grad;
+    float s[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) s[k] = gexp(scale[3 * i + k]);
+    const float4 q = rotation[i];
+    const float qlen = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+    const float4 L0 = l2w[3 * i], L1 = l2w[3 * i + 1], L2 = l2w[3 * i + 2];
+    const float d0 = s[0] * sf + eps, d1 = s[1] * sf + eps, d2 = s[2] * sf + eps;
+    float4 *r = rec + kRecVec * (size_t)i;
+    r[0] = make_float4(lv.x, sf, 1.0f / qlen, s[0]);
+    r[1] = make_float4(s[1], s[2], channels[3 * i], channels[3 * i + 1]);
+    r[2] = make_float4(channels[3 * i + 2], L0.x / d0 * s[0], L0.y / d1 * s[1], L0.z / d2 * s[2]);
+    r[3] = make_float4(L1.x / d0 * s[0], L1.y / d1 * s[1], L1.z / d2 * s[2], L2.x / d0 * s[0]);
+    r[4] = make_float4(L2.y / d1 * s[1], L2.z / d2 * s[2], 0.0f, 0.0f);
+    r[5] = make_float4(q.x / qlen, q.y / qlen, q.z / qlen, q.w / qlen);
+}
+
+// What one composited hit reads: the snapshot rows and the backward record (9 x 16 B).
+struct BwdHit {
+    float4 g0, g1, g2, r0, r1, r2, r3, r4, r5;
+};
+
+__device__ __forceinline__ void load_hit(const BwdArgs &a, uint32_t gid, BwdHit &h) {
+    const float4 *gp = a.geom + 3 * (size_t)gid, *rp = a.rec + kRecVec * (size_t)gid;
+    h.g0 = __ldg(gp);
+    h.g1 = __ldg(gp + 1);
+    h.g2 = __ldg(gp + 2);
+    h.r0 = __ldg(rp);
+    h.r1 = __ldg(rp + 1);
+    h.r2 = __ldg(rp + 2);
+    h.r3 = __ldg(rp + 3);
+    h.r4 = __ldg(rp + 4);
+    h.r5 = __ldg(rp + 5);
+}
+
+// Reverse-order walk of a pixel's segment chain (newest segment first, each segment back to front).
+struct HitCursor {
+    uint32_t seg, prev;
+    int e, guard;
+};
+
+// Next composited gaussian id; false at the end of the list or on a corrupt list (status raised).
+__device__ __forceinline__ bool next_gid(const BwdArgs &a, HitCursor &c, uint32_t &gid) {
+    for (;;) {
+        while (c.e >= 0) {
+            gid = a.pool[c.seg + 2u + (uint32_t)c.e];
+            c.e--;
+            if (gid < (uint32_t)a.n) return true;
+        }
+        if (c.prev == GRAY_NULL) return false;
+        c.seg = c.prev;
+        if (c.seg + 2u > a.pool_size || ++c.guard > kPassSlots * kMaxPasses + 1) {
+            raise_status(a.status, GRAY_STATUS_HITLIST_OVERFLOW);
+            return false;
+        }
+        c.prev = a.pool[c.seg];
+        const uint32_t cnt = a.pool[c.seg + 1];
+        if (cnt > a.pool_size - c.seg - 2u) {
+            raise_status(a.status, GRAY_STATUS_HITLIST_OVERFLOW);
+            return false;
+        }
+        c.e = (int)cnt - 1;
+    }
+}
+
+// Pixel-constant inputs of the replay.
+struct BwdPixel {
+    f3 ro, rd, gout;
+    float Tfin, fT, dbg, drem, inv_npix, pw;
+};
+
+// One step of the reverse replay (cuda/backward_pass.cu:17-137) for hit h; T and gT are the
+// running transmittance and colour-gradient tail.
+__device__ __forceinline__ void replay_hit(const BwdArgs &a, const BwdPixel &px, uint32_t gid, const BwdHit &h,
+                                           float &T, float &gT) {
+    const float o = h.r0.x, sf = h.r0.y, iq = h.r0.z;
+    const f3 s = mk3(h.r0.w, h.r1.x, h.r1.y);
+    const f3 c = mk3(h.r1.z, h.r1.w, h.r2.x);
+    LocalHit lh;
+    local_ray(h.g0, h.g1, h.g2, px.ro, px.rd, lh);
+    closest_point(lh);
+    const f3 x = mk3(lh.u.x * sf, lh.u.y * sf, lh.u.z * sf);
+    const float sq = fdot3(x, x);
+    const float gv = eval_gaussian(sq, px.pw);
+    const float alpha = maxalpha_mul(gv, o);
+
+    const float om = 1.0f - alpha;
+    const float w = T / om * alpha;
+    const float dgc = dot3(px.gout, c);
+    float ga = (dgc - gT) * T / om;
+    ga = ga + -px.fT / om * px.dbg;
+    ga = ga + -((px.Tfin - px.fT) / om) * px.drem;
+    gT = gT + (dgc - gT) * alpha;
+    float go = maxalpha_mul(ga, gv);
+    go = go * o * (1.0f - o);
+    const float ggv = maxalpha_mul(ga, o);
+    float gsq;
+    if (px.pw == 1.0f) gsq = gv;
+    else if (px.pw == 2.0f) gsq = gv * sq;
+    else if (px.pw == 3.0f) gsq = gv * sq * sq;
+    else gsq = gv * gpow(sq, px.pw - 1.0f);
+    const f3 gxl = mk3(-x.x * gsq * ggv, -x.y * gsq * ggv, -x.z * gsq * ggv);
+    const f3 gxw = mk3((h.g0.x * gxl.x + h.g1.x * gxl.y + h.g2.x * gxl.z) * sf,
+                       (h.g0.y * gxl.x + h.g1.y * gxl.y + h.g2.y * gxl.z) * sf,
+                       (h.g0.z * gxl.x + h.g1.z * gxl.y + h.g2.z * gxl.z) * sf);
+    // d loss / d L2W rows: -gxw_r * x
+    const f3 gl0 = mk3(-gxw.x * x.x, -gxw.x * x.y, -gxw.x * x.z);
+    const f3 gl1 = mk3(-gxw.y * x.x, -gxw.y * x.y, -gxw.y * x.z);
+    const f3 gl2 = mk3(-gxw.z * x.x, -gxw.z * x.y, -gxw.z * x.z);
+    const f3 gs = mk3(gl0.x * h.r2.y + gl1.x * h.r3.x + gl2.x * h.r3.w,
+                      gl0.y * h.r2.z + gl1.y * h.r3.y + gl2.y * h.r4.x,
+                      gl0.z * h.r2.w + gl1.z * h.r3.z + gl2.z * h.r4.y);
+    // rotation-matrix gradient and its pull-back to the quaternion through the normalisation
+    const float r00 = gl0.x * s.x, r01 = gl0.y * s.y, r02 = gl0.z * s.z;
+    const float r10 = gl1.x * s.x, r11 = gl1.y * s.y, r12 = gl1.z * s.z;
+    const float r20 = gl2.x * s.x, r21 = gl2.y * s.y, r22 = gl2.z * s.z;
+    const float qw = h.r5.x, qx = h.r5.y, qy = h.r5.z, qz = h.r5.w;
+    const float g_r = 2.0f * qx * (r21 - r12) + 2.0f * qy * (r02 - r20) + 2.0f * qz * (r10 - r01);
+    const float g_x = -4.0f * qx * (r11 + r22) + 2.0f * qy * (r01 + r10) + 2.0f * qz * (r02 + r20) +
+                      2.0f * qw * (r21 - r12);
+    const float g_y = 2.0f * qx * (r01 + r10) - 4.0f * qy * (r00 + r22) + 2.0f * qz * (r12 + r21) +
+                      2.0f * qw * (r02 - r20);
+    const float g_z = 2.0f * qx * (r02 + r20) + 2.0f * qy * (r12 + r21) - 4.0f * qz * (r00 + r11) +
+                      2.0f * qw * (r10 - r01);
+    // (g - (g . qn) qn) / |q| == g / |q| - (g . q) q / |q|^3 (cuda/utils/activations.cu:68-70)
+    const float dq = g_r * qw + g_x * qx + g_y * qy + g_z * qz;
+    float v[16] = {(g_r - dq * qw) * iq, (g_x - dq * qx) * iq, (g_y - dq * qy) * iq, (g_z - dq * qz) * iq,
+                   -gxw.x, -gxw.y, -gxw.z, go, gs.x, gs.y, gs.z, w * px.inv_npix,
+                   px.gout.x * w, px.gout.y * w, px.gout.z * w, 1.0f};
+    reduce_hit(a.grad_acc + 16 * (size_t)gid, gid, v);
+    T = T / om;
+}
+
+// One thread per pixel walks its composited hits back to front (16x8-pixel blocks, so a warp holds
+// two rows of 16 neighbouring pixels).
 __global__ void __launch_bounds__(128) trace_backward_kernel(const BwdArgs a) {
     const int px = blockIdx.x * 16 + (threadIdx.x & 15);
     const int py = blockIdx.y * 8 + (threadIdx.x >> 4);
     if (px >= (int)a.render_w || py >= (int)a.render_h) return;
     const uint32_t pixel = (uint32_t)py * a.alloc_w + (uint32_t)px;
-    uint32_t seg = a.head[pixel];
-    if (seg == GRAY_NULL) return;
-    const float pw = *a.exp_power, eps_sg = *a.eps_scale_grad;
-    const float Tfin = a.pix_T[pixel], fT = a.pix_fullT[pixel];
-    const f3 rem = mk3(a.pix_rem[3 * pixel], a.pix_rem[3 * pixel + 1], a.pix_rem[3 * pixel + 2]);
-    const f3 ro = mk3(a.ray_o[3 * pixel], a.ray_o[3 * pixel + 1], a.ray_o[3 * pixel + 2]);
-    const f3 rd = mk3(a.ray_d[3 * pixel], a.ray_d[3 * pixel + 1], a.ray_d[3 * pixel + 2]);
-    const f3 gout = mk3(a.grad_out[3 * pixel], a.grad_out[3 * pixel + 1], a.grad_out[3 * pixel + 2]);
-    const f3 bg = mk3(a.bg[0], a.bg[1], a.bg[2]);
-    const float dbg = dot3(bg, gout), drem = dot3(rem, gout);
-    const float npix = (float)(a.render_w * a.render_h);
-    float gT = 0.0f, T = Tfin;
-    int guard = 0;
-    while (seg != GRAY_NULL) {
-        if (seg + 2u > a.pool_size || ++guard > kPassSlots * kMaxPasses + 1) {
-            raise_status(a.status, GRAY_STATUS_HITLIST_OVERFLOW);
-            return;
-        }
-        const uint32_t prev = a.pool[seg], cnt = a.pool[seg + 1];
-        if (cnt > a.pool_size - seg - 2u) {
-            raise_status(a.status, GRAY_STATUS_HITLIST_OVERFLOW);
-            return;
-        }
-        for (int e = (int)cnt - 1; e >= 0; e--) {
-            const uint32_t gid = a.pool[seg + 2 + e];
-            if (gid >= (uint32_t)a.n) continue;
-            const float4 g0 = a.geom[3 * gid], g1 = a.geom[3 * gid + 1], g2 = a.geom[3 * gid + 2];
-            const float4 L0 = a.l2w[3 * gid], L1 = a.l2w[3 * gid + 1], L2 = a.l2w[3 * gid + 2];
-            const float2 lv = a.live[gid];
-            const float o = lv.x, sf = lv.y;
-            const f3 s = mk3(gexp(a.scale[3 * gid]), gexp(a.scale[3 * gid + 1]), gexp(a.scale[3 * gid + 2]));
-            const float4 qr = a.rotation[gid];
-            const float qlen = sqrtf(qr.x * qr.x + qr.y * qr.y + qr.z * qr.z + qr.w * qr.w);
-            const float qw = qr.x / qlen, qx = qr.y / qlen, qy = qr.z / qlen, qz = qr.w / qlen;
-            const f3 c = mk3(a.channels[3 * gid], a.channels[3 * gid + 1], a.channels[3 * gid + 2]);
-
-            LocalHit h;
-            local_ray(g0, g1, g2, ro, rd, h);
-            closest_point(h);
-            const f3 x = mk3(h.u.x * sf, h.u.y * sf, h.u.z * sf);
-            const float sq = fdot3(x, x);
-            const float gv = eval_gaussian(sq, pw);
-            const float alpha = maxalpha_mul(gv, o);
-
-            const float om = 1.0f - alpha;
-            const float w = T / om * alpha;
-            const float dgc = dot3(gout, c);
-            float ga = (dgc - gT) * T / om;
-            ga = ga + -fT / om * dbg;
-            ga = ga + -((Tfin - fT) / om) * drem;
-            gT = gT + (dgc - gT) * alpha;
-            float go = maxalpha_mul(ga, gv);
-            go = go * o * (1.0f - o);
-            const float ggv = maxalpha_mul(ga, o);
-            float gsq;
-            if (pw == 1.0f) gsq = gv;
-            else if (pw == 2.0f) gsq = gv * sq;
-            else if (pw == 3.0f) gsq = gv * sq * sq;
-            else gsq = gv * gpow(sq, pw - 1.0f);
-            const f3 gxl = mk3(-x.x * gsq * ggv, -x.y * gsq * ggv, -x.z * gsq * ggv);
-            const f3 gxw = mk3((g0.x * gxl.x + g1.x * gxl.y + g2.x * gxl.z) * sf,
-                               (g0.y * gxl.x + g1.y * gxl.y + g2.y * gxl.z) * sf,
-                               (g0.z * gxl.x + g1.z * gxl.y + g2.z * gxl.z) * sf);
-            // d loss / d L2W rows: -gxw_i * x
-            const f3 gl0 = mk3(-gxw.x * x.x, -gxw.x * x.y, -gxw.x * x.z);
-            const f3 gl1 = mk3(-gxw.y * x.x, -gxw.y * x.y, -gxw.y * x.z);
-            const f3 gl2 = mk3(-gxw.z * x.x, -gxw.z * x.y, -gxw.z * x.z);
-            const f3 den = mk3(s.x * sf + eps_sg, s.y * sf + eps_sg, s.z * sf + eps_sg);
-            const f3 gs = mk3((gl0.x * (L0.x / den.x) + gl1.x * (L1.x / den.x) + gl2.x * (L2.x / den.x)) * s.x,
-                              (gl0.y * (L0.y / den.y) + gl1.y * (L1.y / den.y) + gl2.y * (L2.y / den.y)) * s.y,
-                              (gl0.z * (L0.z / den.z) + gl1.z * (L1.z / den.z) + gl2.z * (L2.z / den.z)) * s.z);
-            // rotation-matrix gradient and its pull-back to the (normalised) quaternion
-            const float r00 = gl0.x * s.x, r01 = gl0.y * s.y, r02 = gl0.z * s.z;
-            const float r10 = gl1.x * s.x, r11 = gl1.y * s.y, r12 = gl1.z * s.z;
-            const float r20 = gl2.x * s.x, r21 = gl2.y * s.y, r22 = gl2.z * s.z;
-            const float g_r = 2.0f * qx * (r21 - r12) + 2.0f * qy * (r02 - r20) + 2.0f * qz * (r10 - r01);
-            const float g_x = -4.0f * qx * (r11 + r22) + 2.0f * qy * (r01 + r10) + 2.0f * qz * (r02 + r20) +
-                              2.0f * qw * (r21 - r12);
-            const float g_y = 2.0f * qx * (r01 + r10) - 4.0f * qy * (r00 + r22) + 2.0f * qz * (r12 + r21) +
-                              2.0f * qw * (r02 - r20);
-            const float g_z = 2.0f * qx * (r02 + r20) + 2.0f * qy * (r12 + r21) - 4.0f * qz * (r00 + r11) +
-                              2.0f * qw * (r10 - r01);
-            const float dq = g_r * qr.x + g_x * qr.y + g_y * qr.z + g_z * qr.w;
-            const float l3 = qlen * qlen * qlen;
-            float *acc = a.grad_acc + 16 * (size_t)gid;
-            red_add4(acc, dq * -qr.x / l3 + g_r / qlen, dq * -qr.y / l3 + g_x / qlen, dq * -qr.z / l3 + g_y / qlen,
-                     dq * -qr.w / l3 + g_z / qlen);
-            red_add4(acc + 4, -gxw.x, -gxw.y, -gxw.z, go);
-            red_add4(acc + 8, gs.x, gs.y, gs.z, w / npix);
-            red_add4(acc + 12, gout.x * w, gout.y * w, gout.z * w, 1.0f);
-            T = T / om;
-        }
-        seg = prev;
+    HitCursor cur;
+    cur.seg = a.head[pixel];
+    if (cur.seg == GRAY_NULL) return;
+    if (cur.seg + 2u > a.pool_size) {
+        raise_status(a.status, GRAY_STATUS_HITLIST_OVERFLOW);
+        return;
     }
+    cur.prev = a.pool[cur.seg];
+    {
+        const uint32_t cnt = a.pool[cur.seg + 1];
+        if (cnt > a.pool_size - cur.seg - 2u) {
+            raise_status(a.status, GRAY_STATUS_HITLIST_OVERFLOW);
+            return;
+        }
+        cur.e = (int)cnt - 1;
+    }
+    cur.guard = 1;
+    BwdPixel P;
+    P.pw = *a.exp_power;
+    P.Tfin = a.pix_T[pixel];
+    P.fT = a.pix_fullT[pixel];
+    const f3 rem = mk3(a.pix_rem[3 * pixel], a.pix_rem[3 * pixel + 1], a.pix_rem[3 * pixel + 2]);
+    P.ro = mk3(a.ray_o[3 * pixel], a.ray_o[3 * pixel + 1], a.ray_o[3 * pixel + 2]);
+    P.rd = mk3(a.ray_d[3 * pixel], a.ray_d[3 * pixel + 1], a.ray_d[3 * pixel + 2]);
+    P.gout = mk3(a.grad_out[3 * pixel], a.grad_out[3 * pixel + 1], a.grad_out[3 * pixel + 2]);
+    const f3 bg = mk3(a.bg[0], a.bg[1], a.bg[2]);
+    P.dbg = dot3(bg, P.gout);
+    P.drem = dot3(rem, P.gout);
+    P.inv_npix = 1.0f / (float)(a.render_w * a.render_h);
+    float gT = 0.0f, T = P.Tfin;
+    uint32_t gid;
+    if (!next_gid(a, cur, gid)) return;
+    do {
+        BwdHit h;
+        load_hit(a, gid, h);
+        replay_hit(a, P, gid, h, T, gT);
+    } while (next_gid(a, cur, gid));
 }
 
 cudaError_t launch_trace_backward(const gray_params &p, cudaStream_t s) {
+    const int n = p.gaussians.count;
+    if (n > 0) {
+        bwd_record_kernel<<<(unsigned int)((n + 255) / 256), 256, 0, s>>>(
+            n, reinterpret_cast<const float2 *>(p.scene.live), p.gaussians.scale,
+            reinterpret_cast<const float4 *>(p.gaussians.rotation), p.gaussians.channels,
+            reinterpret_cast<const float4 *>(p.scene.l2w), p.config.eps_scale_grad,
+            reinterpret_cast<float4 *>(p.scene.bwd_rec));
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     BwdArgs a;
     a.alloc_w = p.image_width;
     a.render_w = p.render_width;
     a.render_h = p.render_height;
-    a.n = p.gaussians.count;
+    a.n = n;
     a.exp_power = p.config.exp_power;
     a.alpha_threshold = p.config.alpha_threshold;
     a.eps_scale_grad = p.config.eps_scale_grad;
     a.bg = p.config.background_channels;
     a.geom = reinterpret_cast<const float4 *>(p.scene.geom);
-    a.l2w = reinterpret_cast<const float4 *>(p.scene.l2w);
-    a.live = reinterpret_cast<const float2 *>(p.scene.live);
-    a.scale = p.gaussians.scale;
-    a.channels = p.gaussians.channels;
-    a.rotation = reinterpret_cast<const float4 *>(p.gaussians.rotation);
+    a.rec = reinterpret_cast<const float4 *>(p.scene.bwd_rec);
     a.pix_T = p.framebuffer.transmittance;
     a.pix_fullT = p.framebuffer.full_transmittance;
     a.pix_rem = p.framebuffer.remaining_channels_estimate;

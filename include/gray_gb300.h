@@ -143,6 +143,8 @@ typedef struct gray_scene {
     uint32_t *sort_tmp;   /* [sort_tmp_words] */
     float *root_box;      /* [8] */
     uint32_t *bounds;     /* [8] order-preserving encoded scene bounds (scratch) */
+    float *bwd_rec;       /* [N,24] per-Gaussian backward record, written at the start of each
+                             backward pass (training tracers; may be NULL for inference) */
     int32_t bvh_valid;    /* host flag: a rebuild has been done for this count */
 } gray_scene;
 

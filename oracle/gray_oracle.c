@@ -18,6 +18,8 @@
  * Deliberate, documented differences from the reference (shared with the CUDA path):
  *   - the all-hit "skipped" sums (forward_pass.cu:50-56, 92-93) are accumulated exactly in
  *     64-bit fixed point instead of an order-dependent fp32 running sum;
+ *   - the full transmittance (shaders.cu:55-56, an fp32 product in traversal order) is the
+ *     exponential of a fixed-point sum of log(1 - alpha), so it does not depend on the order;
  *   - hits with equal fp16 distance are ordered by gaussian id (the reference uses OptiX
  *     traversal order, which is not reproducible);
  *   - IEEE division/sqrt and this file's own exp/log instead of --use_fast_math intrinsics;
@@ -658,6 +660,7 @@ static int cmp_u64(const void *a, const void *b) {
 }
 
 typedef struct {
+    int64_t lfx; /* sum of log(1 - alpha) in 2^-40 fixed point (full transmittance) */
     float ft;
     int64_t afx, cfx[3];
     int32_t nhit;
@@ -673,9 +676,18 @@ static inline int64_t to_fixed(float v, float scale) {
     return (int64_t)t;
 }
 
+/* Full transmittance prod(1 - alpha) (cuda/shaders.cu:55-56 multiplies in traversal order) kept
+ * order-independent: log(1 - alpha) summed in 2^-40 fixed point, exponentiated once per ray; below
+ * -105 (exp underflows to 0) no further terms are added. */
+#define LOG_FIX_FLOOR (-105LL * (1LL << 40))
+static inline void add_log_transmittance(int64_t *s, float alpha) {
+    if (*s > LOG_FIX_FLOOR) *s += to_fixed(orc_logf(1.0f - alpha), 0x1.0p40f);
+}
+static inline float full_transmittance(int64_t s) { return orc_expf((float)s * 0x1.0p-40f); }
+
 static inline void record_hit(hit_acc *acc, ray_scratch *scr, uint32_t gid, is_result h, const float *channels,
                               float znear) {
-    acc->ft = fmaf(-acc->ft, h.alpha, acc->ft);
+    add_log_transmittance(&acc->lfx, h.alpha);
     uint16_t a16 = orc_f2h(h.alpha), d16 = orc_f2h(h.dist);
     float af = orc_h2f(a16);
     const float *c = channels + 3 * (size_t)gid;
@@ -715,7 +727,7 @@ typedef struct {
 static void trace_one(fwd_job *J, int r, ray_scratch *scr) {
     const orc_trace_cfg *cfg = J->cfg;
     const float *ro = J->ray_o + 3 * (size_t)r, *rd = J->ray_d + 3 * (size_t)r;
-    hit_acc acc = {1.0f, 0, {0, 0, 0}, 0};
+    hit_acc acc = {0, 1.0f, 0, {0, 0, 0}, 0};
     scr->n = 0;
     if (rd[0] == 0.0f && rd[1] == 0.0f && rd[2] == 0.0f) {
         /* inactive pixel (cuda/shaders.cu:86-88): nothing is written */
@@ -806,6 +818,7 @@ static void trace_one(fwd_job *J, int r, ray_scratch *scr) {
         nacc++;
         if (T < cfg->t_threshold) break;
     }
+    acc.ft = full_transmittance(acc.lfx);
     float rT = T - acc.ft;
     float rem[3] = {0.0f, 0.0f, 0.0f};
     if (acc.afx > 0) {

@@ -16,7 +16,6 @@ from tests import gpu_util as G
 
 pytestmark = pytest.mark.gpu
 
-RGB_TOL = 2e-6        # colour: order of the full-transmittance product only
 GRAD_RTOL = 1e-4      # gradients: fp32 atomics vs the oracle's double accumulation
 
 
@@ -46,8 +45,8 @@ def _compare_forward(rt, fwd, check_lists=True):
     same("nacc", nacc[alive], fwd["nacc"][alive])
     same("T", f["transmittance"][alive, 0], fwd["T"][alive])
     same("rem", f["remaining_channels_estimate"][alive], fwd["rem"][alive])
-    assert np.allclose(f["full_transmittance"][alive, 0], fwd["fullT"][alive], rtol=2e-6, atol=1e-7)
-    assert np.abs(f["output_channels"][alive] - fwd["rgb"][alive]).max() < RGB_TOL
+    same("fullT", f["full_transmittance"][alive, 0], fwd["fullT"][alive])
+    same("rgb", f["output_channels"][alive], fwd["rgb"][alive])
     if check_lists:
         gl, ol = G.hit_lists(rt), G.oracle_lists(fwd)
         for i in np.nonzero(alive)[0]:
@@ -188,7 +187,8 @@ def test_multipass_selection_and_segments(oracle):
     n = 3000
     mean = np.stack([rng.normal(0, 0.15, n), rng.normal(0, 0.15, n), rng.uniform(-3, 3, n)], 1).astype(np.float32)
     rot = rng.standard_normal((n, 4)).astype(np.float32)
-    scale = np.full((n, 3), math.log(0.3), np.float32)
+    # anisotropic, so that the rotation gradient is not zero (for spheres it is rounding noise)
+    scale = rng.uniform(math.log(0.15), math.log(0.45), (n, 3)).astype(np.float32)
     opac = np.full((n, 1), -2.5, np.float32)  # sigmoid ~ 0.076
     chan = rng.uniform(0, 1, (n, 3)).astype(np.float32)
     W = H = 24
@@ -240,7 +240,7 @@ def test_znear_zfar_and_render_rectangle(oracle):
     fwd = oracle.trace_forward(f["ray_origin"][idx], f["ray_direction"][idx], geom, live, chan, vis, cfg)
     assert np.array_equal(f["transmittance"][idx, 0], fwd["T"])
     assert np.array_equal(f["output_depth"][idx, 0], fwd["depth"])
-    assert np.abs(f["output_channels"][idx] - fwd["rgb"]).max() < RGB_TOL
+    assert np.array_equal(f["output_channels"][idx], fwd["rgb"])
     lists = G.hit_lists(rt)
     ol = G.oracle_lists(fwd)
     for k, i in enumerate(idx):
