@@ -126,9 +126,12 @@ def measured_peak_gbs():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel):
+def ncu_traffic(kernel, a):
+    """DRAM bytes (read + write) of one launch of `kernel` on this workload, from an ncu capture
+    summarised in profiles/ncu_traffic.json (key "<kernel> <gaussians> <width>x<height>")."""
     try:
-        return json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json"))).get(kernel)
+        table = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
+        return table.get(f"{kernel} {a.n_gaussians} {a.width}x{a.height}")
     except Exception:
         return None
 
@@ -251,7 +254,7 @@ def gpu_arm(a, rank, world, local_rank):
     launches = sum(cnt * kernels_per_group.get(name, 1) for name, (_, cnt) in res.items())
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "traffic": ncu_traffic(dominant), "algorithmic_bytes": algo.get(dominant),
+                "traffic": ncu_traffic(dominant, a), "algorithmic_bytes": algo.get(dominant),
                 "avg_launch_ms": round(dom_ms, 4),
                 "shares": {k: round(v[0] / total_ms, 4) for k, v in sorted(res.items(), key=lambda kv: -kv[1][0])},
                 "hits_per_ray": round(H / R, 2), "composited_per_ray": round(A / R, 2)}

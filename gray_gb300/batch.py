@@ -25,7 +25,7 @@ from .camera import CameraInfo
 
 class BatchSceneC(ctypes.Structure):
     _fields_ = [("geom", ctypes.c_void_p), ("live", ctypes.c_void_p), ("nodes", ctypes.c_void_p),
-                ("root_box", ctypes.c_void_p), ("n", ctypes.c_int32), ("exp_power", ctypes.c_float),
+                ("root_box", ctypes.c_void_p), ("l2w", ctypes.c_void_p), ("n", ctypes.c_int32), ("exp_power", ctypes.c_float),
                 ("alpha_threshold", ctypes.c_float), ("t_threshold", ctypes.c_float), ("bg", ctypes.c_float * 3),
                 ("pad", ctypes.c_int32)]
 
@@ -58,10 +58,13 @@ def _check(L, rc, what):
         raise _lib.GrayError(f"{what}: {L.gray_last_error().decode()} (code {rc})")
 
 
-# untuned choice: 4x8 packets with a 16-entry k-buffer (the library's default variant), 8 blocks per SM
-DEFAULT_VARIANT, DEFAULT_BLOCKS_PER_SM = 7, 8
-# candidates the autotuner tries: (kernel variant, persistent blocks per SM)
-TUNE_CANDIDATES = [(v, b) for v in (1, 2, 3, 5, 7) for b in (4, 6, 8)]
+# untuned choice: 4x8 packets with a 16-entry k-buffer (the library's default variant), as many
+# blocks per SM as its shared memory and register cap allow (7)
+DEFAULT_VARIANT, DEFAULT_BLOCKS_PER_SM = 7, 7
+# candidates the autotuner tries: (kernel variant, persistent blocks per SM), each variant with the
+# block counts around its residency limit (32-entry buffers: 4 per SM; 16 entries uncapped: 3;
+# 16 entries capped: 7)
+TUNE_CANDIDATES = [(1, 4), (5, 4), (2, 3), (6, 3), (3, 6), (3, 7), (7, 6), (7, 7)]
 
 
 @dataclass
@@ -107,14 +110,14 @@ class BatchRenderer:
         for t in self.tracers:
             ws = t.scene_workspace()
             ptrs.append((ws.geom.data_ptr(), ws.live.data_ptr(), ws.nodes.data_ptr(), ws.root_box.data_ptr(),
-                         t.get_gaussians().count))
+                         ws.l2w.data_ptr(), t.get_gaussians().count))
         if self._scenes_dev is not None and ptrs == self._scene_ptrs:
             return self._scenes_dev
         arr = (BatchSceneC * len(self.tracers))()
         for i, t in enumerate(self.tracers):
             cfg = t.get_config()
-            g, lv, nd, rb, n = ptrs[i]
-            arr[i].geom, arr[i].live, arr[i].nodes, arr[i].root_box, arr[i].n = g, lv, nd, rb, n
+            g, lv, nd, rb, lw, n = ptrs[i]
+            arr[i].geom, arr[i].live, arr[i].nodes, arr[i].root_box, arr[i].l2w, arr[i].n = g, lv, nd, rb, lw, n
             arr[i].exp_power = float(cfg.exp_power.item())
             arr[i].alpha_threshold = float(cfg.alpha_threshold.item())
             arr[i].t_threshold = float(cfg.t_threshold.item())

@@ -130,12 +130,23 @@ __device__ __forceinline__ float adam_pow(float beta, int n) {
     return (float)r;
 }
 
-// Fixed-point form of one all-hit sum term: v * scale truncated toward zero (clamped, NaN -> 0).
+// Fixed-point form of one all-hit sum term: v * scale (scale a power of two) truncated toward
+// zero, clamped to +-2^62, NaN -> 0.  Decoded from the float's bits with integer operations only
+// (a float-to-int64 conversion would go through the FP64 unit, which is narrow on GB300):
+// |t| = m 2^(e-150) with m the 24-bit significand, so trunc(|t|) = m << (e-150) or m >> (150-e).
 __device__ __forceinline__ long long to_fixed(float v, float scale) {
-    float t = v * scale;
-    if (!(t == t)) t = 0.0f;
-    t = fminf(fmaxf(t, -0x1.0p62f), 0x1.0p62f);
-    return __float2ll_rz(t);
+    const uint32_t b = __float_as_uint(v * scale);
+    const uint32_t e = (b >> 23) & 0xFFu;
+    if (e < 127u) return 0;                                // |t| < 1 (zero, subnormal)
+    if (e == 0xFFu && (b & 0x7FFFFFu)) return 0;           // NaN
+    unsigned long long mag;
+    if (e >= 189u) {
+        mag = 1ull << 62;                                  // |t| >= 2^62 (inf included)
+    } else {
+        const unsigned long long m = (unsigned long long)((b & 0x7FFFFFu) | 0x800000u);
+        mag = e >= 150u ? m << (e - 150u) : m >> (150u - e);
+    }
+    return (b >> 31) ? -(long long)mag : (long long)mag;
 }
 
 __device__ __forceinline__ uint16_t f2h_bits(float f) { return __half_as_ushort(__float2half_rn(f)); }
@@ -221,6 +232,20 @@ __device__ __forceinline__ void add_log_transmittance(long long &s, float alpha)
     if (s > kLogFixFloor) s += to_fixed(glog(1.0f - alpha), 0x1.0p40f);
 }
 __device__ __forceinline__ float full_transmittance(long long s) { return gexp(__ll2float_rn(s) * 0x1.0p-40f); }
+
+// The hit decision of intersect() alone (same arithmetic, so the same answer), without the
+// Gaussian response.
+__device__ __forceinline__ bool intersect_hits(const float4 g0, const float4 g1, const float4 g2, float o, f3 ro,
+                                               f3 rd, float alpha_threshold, float znear, float zfar) {
+    if (o <= alpha_threshold) return false;
+    LocalHit h;
+    local_ray(g0, g1, g2, ro, rd, h);
+    if (h.b > 0.0f) return false;
+    closest_point(h);
+    if (fdot3(h.u, h.u) > 1.0f) return false;
+    if (!(h.t >= znear && h.t <= zfar)) return unit_box_overlap(h, znear, zfar);
+    return true;
+}
 
 // alpha * 2^24 for an fp16 alpha in [0, 1): an exact integer, from the half's bits
 __device__ __forceinline__ long long alpha16_fixed(uint16_t a16) {

@@ -126,7 +126,7 @@ __global__ void snapshot_kernel(int n, const float *__restrict__ mean, const flo
         gr.z = vis ? R[6 + rr] / s[rr] : 0.0f;
         gr.w = mu[rr];
         geom[3 * i + rr] = gr;
-        l2w[3 * i + rr] = make_float4(L[3 * rr], L[3 * rr + 1], L[3 * rr + 2], 0.0f);
+        l2w[3 * i + rr] = make_float4(L[3 * rr], L[3 * rr + 1], L[3 * rr + 2], mu[rr]);
     }
     float4 bmin, bmax;
     if (vis) {

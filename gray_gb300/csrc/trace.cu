@@ -29,8 +29,9 @@ constexpr int kPassSlots = 32;               // BUFFER_SIZE, cuda/forward_pass.c
 constexpr int kMaxPasses = 99;               // MAX_ITERATIONS, cuda/forward_pass.cu:3
 constexpr int kMaxTraversals = 4 * kMaxPasses * 2;  // bound on re-traversals of one ray
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kWideStack = 512;  // per-warp shared stack of the frustum traversal
-constexpr int kCand = 64;        // per-warp candidate leaves between flushes
+constexpr int kWideStack = 256;  // per-warp shared stack of the frustum traversal
+constexpr int kCand = 32;        // leaves processed per flush (one per lane)
+constexpr int kQueue = 3 * kCand; // per-warp queue of leaves: < kCand before a step, + up to 64 per step
 
 struct FwdArgs {
     uint32_t alloc_w, render_w, render_h;
@@ -43,7 +44,7 @@ struct FwdArgs {
     const float *ellipsoid_min_opacity;
     int display;  // forward_pass_display: colour only, whatever grads_enabled holds
     const uint32_t *total_num_calls;
-    const float4 *geom;
+    const float4 *geom, *l2w;
     const float2 *live;
     const float *channels;
     const float4 *nodes;
@@ -110,6 +111,7 @@ struct LaneState {
 // What one ray traces against.
 struct TraceScene {
     const float4 *geom;
+    const float4 *l2w;  // rows (L | mu) for the leaf cull of the frustum traversal (may be null)
     const float2 *live;
     const float *channels;
     const float4 *nodes;
@@ -135,23 +137,23 @@ struct RayResult {
     uint32_t head;
 };
 
+// Intersection program + all-hit sums + selection for one (ray, Gaussian) pair whose snapshot rows,
+// live values and colour the caller has fetched.
 template <int KB>
-__device__ __forceinline__ void on_leaf(const TraceScene &sc, uint32_t gid, bool want, bool first, f3 ro, f3 rd,
-                                        const TraceKnobs &k, LaneState &st, unsigned long long (*kbuf)[kFwdThreads]) {
-    if (!want) return;
-    const float4 g0 = sc.geom[3 * gid], g1 = sc.geom[3 * gid + 1], g2 = sc.geom[3 * gid + 2];
-    const float2 lv = sc.live[gid];
+__device__ __forceinline__ void on_leaf_data(uint32_t gid, const float4 g0, const float4 g1, const float4 g2,
+                                             const float2 lv, float c0, float c1, float c2, bool first, f3 ro,
+                                             f3 rd, const TraceKnobs &k, LaneState &st,
+                                             unsigned long long (*kbuf)[kFwdThreads]) {
     float dist, alpha;
     if (!intersect(g0, g1, g2, lv.x, lv.y, ro, rd, k.athr, k.pw, k.znear, k.zfar, dist, alpha)) return;
     const uint16_t a16 = f2h_bits(alpha), d16 = f2h_bits(dist);
     if (first) {
         add_log_transmittance(st.lfx, alpha);
         const float af = h2f_bits(a16);
-        const float *c = sc.channels + 3 * (size_t)gid;
         st.afx += alpha16_fixed(a16);
-        st.cfx0 += to_fixed(af * c[0], 0x1.0p32f);
-        st.cfx1 += to_fixed(af * c[1], 0x1.0p32f);
-        st.cfx2 += to_fixed(af * c[2], 0x1.0p32f);
+        st.cfx0 += to_fixed(af * c0, 0x1.0p32f);
+        st.cfx1 += to_fixed(af * c1, 0x1.0p32f);
+        st.cfx2 += to_fixed(af * c2, 0x1.0p32f);
         st.nhit++;
     }
     if (!(h2f_bits(d16) > k.znear)) return;
@@ -177,6 +179,25 @@ __device__ __forceinline__ void on_leaf(const TraceScene &sc, uint32_t gid, bool
     kbuf[pos][t] = key;
     if (st.kcount == KB) st.kmax = kbuf[KB - 1][t];
 }
+
+template <int KB>
+__device__ __forceinline__ void on_leaf(const TraceScene &sc, uint32_t gid, bool want, bool first, f3 ro, f3 rd,
+                                        const TraceKnobs &k, LaneState &st, unsigned long long (*kbuf)[kFwdThreads]) {
+    if (!want) return;
+    // every load up front (the colour too): one memory round trip per hit
+    const float4 g0 = sc.geom[3 * gid], g1 = sc.geom[3 * gid + 1], g2 = sc.geom[3 * gid + 2];
+    const float2 lv = sc.live[gid];
+    const float *cp = sc.channels + 3 * (size_t)gid;
+    on_leaf_data<KB>(gid, g0, g1, g2, lv, cp[0], cp[1], cp[2], first, ro, rd, k, st, kbuf);
+}
+
+// Per-warp shared-memory copy of the queued leaves' records, filled once per flush by the lanes
+// (one candidate each, all loads in flight together) and read by every lane afterwards.
+struct CandCache {
+    float4 g[kCand][3];  // snapshot rows (M | mu)
+    float4 c[kCand];     // colour, live opacity
+    float sf[kCand];     // live scaling factor
+};
 
 __device__ __forceinline__ void stack_push(uint32_t &stk0, uint32_t &stk1, int &sp, uint32_t v, int lane,
                                            int32_t *status) {
@@ -237,6 +258,90 @@ __device__ __forceinline__ bool frustum_box(const Frustum &fr, const float bmin[
     return true;
 }
 
+// Conservative frustum test of a Gaussian's support ellipsoid {mu + L u : |u| <= 1} (L, mu = the
+// snapshot's l2w rows): false only when the ellipsoid lies outside one plane by more than a rounding
+// margin.  The ellipsoid's extent along a normal n is |L^T n|.  A ray can only hit a Gaussian whose
+// ellipsoid it crosses, so a leaf whose ellipsoid misses the packet's frustum holds no hit of the
+// packet even when its box passed.
+__device__ __forceinline__ bool frustum_ellipsoid(const Frustum &fr, const float4 *l2w) {
+    const float4 r0 = l2w[0], r1 = l2w[1], r2 = l2w[2];
+    const float vx = r0.w - fr.o[0], vy = r1.w - fr.o[1], vz = r2.w - fr.o[2];
+#pragma unroll
+    for (int p = 0; p < 5; p++) {
+        const float nx = fr.n[p][0], ny = fr.n[p][1], nz = fr.n[p][2];
+        const float sdist = fmaf(nz, vz, fmaf(ny, vy, nx * vx));
+        const float e0 = fmaf(r2.x, nz, fmaf(r1.x, ny, r0.x * nx));
+        const float e1 = fmaf(r2.y, nz, fmaf(r1.y, ny, r0.y * nx));
+        const float e2 = fmaf(r2.z, nz, fmaf(r1.z, ny, r0.z * nx));
+        const float ext = sqrtf(fmaf(e2, e2, fmaf(e1, e1, e0 * e0)));
+        const float n1 = fabsf(nx) + fabsf(ny) + fabsf(nz);
+        const float margin = 1e-5f * (n1 * (fabsf(vx) + fabsf(vy) + fabsf(vz)) + 3.0f * ext) + 1e-30f;
+        if (sdist + ext < -margin) return false;
+    }
+    return true;
+}
+
+// Processes the packet's queued leaves (cand[0, nc), at most kCand = 32; every lane of the warp calls
+// this together).  (1) Lane j takes candidate j: it tests the candidate's ellipsoid against the
+// packet frustum and fetches its snapshot rows, live values and colour; the survivors are
+// compacted into the warp's shared-memory cache.  (2) Every lane runs the hit test of its own ray
+// against every cached candidate and keeps a 32-bit mask of its hits.  (3) The lanes walk their
+// masks together, one hit per lane per step, through the intersection program and the selection.
+// The order in which a lane sees its hits does not matter: the all-hit sums are order-independent
+// and the selection is by key.
+template <int KB>
+__device__ __forceinline__ void flush_candidates(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool want,
+                                                 bool first, LaneState &st, unsigned long long (*kbuf)[kFwdThreads],
+                                                 const Frustum &fr, uint32_t *cand, CandCache &cc, int nc) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lanemask_lt = (1u << lane) - 1u;
+    uint32_t gid = 0;
+    bool keep = false;
+    float4 g0, g1, g2, cv;
+    float sfv = 0.0f;
+    if (lane < nc) {
+        gid = cand[lane];
+        g0 = sc.geom[3 * (size_t)gid];
+        g1 = sc.geom[3 * (size_t)gid + 1];
+        g2 = sc.geom[3 * (size_t)gid + 2];
+        const float2 lv = sc.live[gid];
+        const float *cp = sc.channels + 3 * (size_t)gid;
+        cv = make_float4(cp[0], cp[1], cp[2], lv.x);
+        sfv = lv.y;
+        keep = sc.l2w ? frustum_ellipsoid(fr, sc.l2w + 3 * (size_t)gid) : true;
+    }
+    const uint32_t bal = __ballot_sync(kFull, keep);
+    __syncwarp();  // every read of cand[] precedes the compacting writes
+    if (keep) {
+        const int slot = __popc(bal & lanemask_lt);
+        cand[slot] = gid;
+        cc.g[slot][0] = g0;
+        cc.g[slot][1] = g1;
+        cc.g[slot][2] = g2;
+        cc.c[slot] = cv;
+        cc.sf[slot] = sfv;
+    }
+    nc = __popc(bal);
+    __syncwarp();
+    uint32_t mask = 0u;
+    if (want) {
+        for (int j = 0; j < nc; j++) {
+            if (intersect_hits(cc.g[j][0], cc.g[j][1], cc.g[j][2], cc.c[j].w, ro, rd, k.athr, k.znear, k.zfar))
+                mask |= 1u << j;
+        }
+    }
+    while (__any_sync(kFull, mask != 0u)) {
+        if (mask != 0u) {
+            const int j = __ffs(mask) - 1;
+            mask &= mask - 1u;
+            const float4 c = cc.c[j];
+            on_leaf_data<KB>(cand[j], cc.g[j][0], cc.g[j][1], cc.g[j][2], make_float2(c.w, cc.sf[j]), c.x, c.y,
+                             c.z, first, ro, rd, k, st, kbuf);
+        }
+    }
+    __syncwarp();
+}
+
 // One full traversal of the packet (camera rays with a common origin) with the node work spread
 // over the lanes: each step pops up to 32 nodes, one per lane, tests their child boxes against the
 // packet frustum, pushes surviving internal children and queues surviving leaves; queued leaves
@@ -246,7 +351,7 @@ template <int KB>
 __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool want,
                                                  bool first, LaneState &st, unsigned long long (*kbuf)[kFwdThreads],
                                                  const Frustum &fr, uint32_t *stk, uint32_t *cand,
-                                                 int32_t *status) {
+                                                 CandCache &cc, int32_t *status) {
     const int lane = threadIdx.x & 31;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     const int n = sc.n;
@@ -260,61 +365,73 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
     if (lane == 0) stk[0] = 0u;
     __syncwarp();
     int sp = 1, nc = 0;
-    bool ok = true;
+    bool ok = true, draining = false;
     long long budget = (long long)n;  // a valid tree pushes each internal node at most once per traversal
-    while (sp > 0) {
-        if (--budget < 0) {
-            raise_status(status, GRAY_STATUS_STACK_OVERFLOW);
-            break;
-        }
-        const int take = sp < 32 ? sp : 32;
-        uint32_t node = GRAY_NULL;
-        if (lane < take) node = stk[sp - 1 - lane];
-        __syncwarp();
-        sp -= take;
-        bool p0 = false, p1 = false;
-        uint32_t c0 = 0, c1 = 0;
-        if (node != GRAY_NULL) {
-            if (node >= (uint32_t)(n - 1)) {
+    for (;;) {
+        if (!draining) {
+            if (sp == 0) {
+                draining = true;
+            } else if (--budget < 0) {
                 raise_status(status, GRAY_STATUS_STACK_OVERFLOW);
+                draining = true;
             } else {
-                const float4 q0 = sc.nodes[4 * node], q1 = sc.nodes[4 * node + 1], q2 = sc.nodes[4 * node + 2],
-                             q3 = sc.nodes[4 * node + 3];
-                const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
-                const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
-                c0 = __float_as_uint(q3.x);
-                c1 = __float_as_uint(q3.y);
-                p0 = frustum_box(fr, b0min, b0max);
-                p1 = frustum_box(fr, b1min, b1max);
+                const int take = sp < 32 ? sp : 32;
+                uint32_t node = GRAY_NULL;
+                if (lane < take) node = stk[sp - 1 - lane];
+                __syncwarp();
+                sp -= take;
+                bool p0 = false, p1 = false;
+                uint32_t c0 = 0, c1 = 0;
+                if (node != GRAY_NULL) {
+                    if (node >= (uint32_t)(n - 1)) {
+                        raise_status(status, GRAY_STATUS_STACK_OVERFLOW);
+                    } else {
+                        const float4 q0 = sc.nodes[4 * node], q1 = sc.nodes[4 * node + 1],
+                                     q2 = sc.nodes[4 * node + 2], q3 = sc.nodes[4 * node + 3];
+                        const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
+                        const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
+                        c0 = __float_as_uint(q3.x);
+                        c1 = __float_as_uint(q3.y);
+                        p0 = frustum_box(fr, b0min, b0max);
+                        p1 = frustum_box(fr, b1min, b1max);
+                    }
+                }
+                const bool i0 = p0 && !(c0 & GRAY_LEAF_BIT), i1 = p1 && !(c1 & GRAY_LEAF_BIT);
+                const bool l0 = p0 && (c0 & GRAY_LEAF_BIT) && (c0 & ~GRAY_LEAF_BIT) < (uint32_t)n;
+                const bool l1 = p1 && (c1 & GRAY_LEAF_BIT) && (c1 & ~GRAY_LEAF_BIT) < (uint32_t)n;
+                const uint32_t m0 = __ballot_sync(kFull, i0), m1 = __ballot_sync(kFull, i1);
+                const int n0 = __popc(m0), n1 = __popc(m1);
+                if (sp + n0 + n1 > kWideStack) {
+                    ok = false;  // frontier too wide for the shared stack
+                    break;
+                }
+                if (i0) stk[sp + __popc(m0 & lanemask_lt)] = c0;
+                if (i1) stk[sp + n0 + __popc(m1 & lanemask_lt)] = c1;
+                sp += n0 + n1;
+                // queue the leaves found (nc < kCand before the step, at most 64 added)
+                const uint32_t q0m = __ballot_sync(kFull, l0), q1m = __ballot_sync(kFull, l1);
+                const int lq0 = __popc(q0m);
+                if (l0) cand[nc + __popc(q0m & lanemask_lt)] = c0 & ~GRAY_LEAF_BIT;
+                if (l1) cand[nc + lq0 + __popc(q1m & lanemask_lt)] = c1 & ~GRAY_LEAF_BIT;
+                nc += lq0 + __popc(q1m);
+                __syncwarp();
             }
         }
-        const bool i0 = p0 && !(c0 & GRAY_LEAF_BIT), i1 = p1 && !(c1 & GRAY_LEAF_BIT);
-        const bool l0 = p0 && (c0 & GRAY_LEAF_BIT) && (c0 & ~GRAY_LEAF_BIT) < (uint32_t)n;
-        const bool l1 = p1 && (c1 & GRAY_LEAF_BIT) && (c1 & ~GRAY_LEAF_BIT) < (uint32_t)n;
-        const uint32_t m0 = __ballot_sync(kFull, i0), m1 = __ballot_sync(kFull, i1);
-        const int n0 = __popc(m0), n1 = __popc(m1);
-        if (sp + n0 + n1 > kWideStack) {
-            ok = false;  // frontier too wide for the shared stack
-            break;
-        }
-        if (i0) stk[sp + __popc(m0 & lanemask_lt)] = c0;
-        if (i1) stk[sp + n0 + __popc(m1 & lanemask_lt)] = c1;
-        sp += n0 + n1;
-        const uint32_t q0m = __ballot_sync(kFull, l0), q1m = __ballot_sync(kFull, l1);
-        const int lq0 = __popc(q0m), lq1 = __popc(q1m);
-        if (nc + lq0 + lq1 > kCand) {
+        // keep the queue below kCand before the next step (a step adds at most 64 < kQueue - kCand)
+        while (nc >= kCand || (draining && nc > 0)) {
+            // process the first kCand queued leaves, then move the rest to the front
+            const int take = nc < kCand ? nc : kCand;
+            flush_candidates<KB>(sc, k, ro, rd, want, first, st, kbuf, fr, cand, cc, take);
+            const int rest = nc - take;
+            const uint32_t r0 = lane < rest ? cand[kCand + lane] : 0u;
+            const uint32_t r1 = lane + 32 < rest ? cand[kCand + 32 + lane] : 0u;
             __syncwarp();
-            for (int j = 0; j < nc; j++) on_leaf<KB>(sc, cand[j], want, first, ro, rd, k, st, kbuf);
+            if (lane < rest) cand[lane] = r0;
+            if (lane + 32 < rest) cand[32 + lane] = r1;
             __syncwarp();
-            nc = 0;
+            nc = rest;
         }
-        if (l0) cand[nc + __popc(q0m & lanemask_lt)] = c0 & ~GRAY_LEAF_BIT;
-        if (l1) cand[nc + lq0 + __popc(q1m & lanemask_lt)] = c1 & ~GRAY_LEAF_BIT;
-        nc += lq0 + lq1;
-        __syncwarp();
-    }
-    if (ok) {
-        for (int j = 0; j < nc; j++) on_leaf<KB>(sc, cand[j], want, first, ro, rd, k, st, kbuf);
+        if (draining) break;
     }
     __syncwarp();
     return ok;
@@ -328,7 +445,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
                                           bool grads, const HitSink &hs, int32_t *status,
                                           unsigned long long (*kbuf)[kFwdThreads], RayResult &res,
                                           const Frustum *fr = nullptr, uint32_t *wstk = nullptr,
-                                          uint32_t *wcand = nullptr) {
+                                          uint32_t *wcand = nullptr, CandCache *wcc = nullptr) {
     const int lane = threadIdx.x & 31;
     LaneState &st = res.st;
     st.lfx = 0;
@@ -364,7 +481,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
         st.ncand = 0;
         // ---------------- traversal ----------------
         bool per_ray = fr == nullptr;
-        if (!per_ray && !traverse_frustum<KB>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, status)) {
+        if (!per_ray && !traverse_frustum<KB>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, *wcc, status)) {
             // the frustum traversal gave up (stack overflow): discard what it gathered, trace per ray
             st.kcount = 0;
             st.ncand = 0;
@@ -588,7 +705,8 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const 
     __shared__ unsigned long long kbuf[KB][kFwdThreads];
     __shared__ Frustum sfr[kWarps];
     __shared__ uint32_t sstk[kWarps][kWideStack];
-    __shared__ uint32_t scand[kWarps][kCand];
+    __shared__ uint32_t scand[kWarps][kQueue];
+    __shared__ CandCache scc[kWarps];
     if (*a.render_ellipsoids) return;  // the ellipsoid view (ellipsoid_kernel) renders this frame
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int px = blockIdx.x * (a.tile_w * kBlockWarpsX) + (warp % kBlockWarpsX) * a.tile_w + (lane % a.tile_w);
@@ -604,7 +722,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const 
     k.tthr = *a.t_threshold;
     k.render_depth = *a.render_depth != 0;
     const bool grads = !a.display && *a.grads_enabled != 0;
-    const TraceScene sc{a.geom, a.live, a.channels, a.nodes, a.root_box, a.n};
+    const TraceScene sc{a.geom, a.l2w, a.live, a.channels, a.nodes, a.root_box, a.n};
     const HitSink hs{a.counter, a.pool, a.pool_size};
 
     // ---- ray generation (cuda/shaders.cu:76-88) ----
@@ -644,7 +762,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const 
     }
     RayResult r;
     trace_ray<KB>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sstk[warp],
-                  scand[warp]);
+                  scand[warp], &scc[warp]);
 
     if (!inside) return;
     if (!alive) {
@@ -870,7 +988,8 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
     __shared__ unsigned long long kbuf[KB][kFwdThreads];
     __shared__ Frustum sfr[kWarps];
     __shared__ uint32_t sstk[kWarps][kWideStack];
-    __shared__ uint32_t scand[kWarps][kCand];
+    __shared__ uint32_t scand[kWarps][kQueue];
+    __shared__ CandCache scc[kWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tile_h = 32 / tile_w;
     for (;;) {
@@ -895,7 +1014,8 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
         k.pw = bs.exp_power;
         k.tthr = bs.t_threshold;
         k.render_depth = false;
-        const TraceScene sc{reinterpret_cast<const float4 *>(bs.geom), reinterpret_cast<const float2 *>(bs.live),
+        const TraceScene sc{reinterpret_cast<const float4 *>(bs.geom), reinterpret_cast<const float4 *>(bs.l2w),
+                            reinterpret_cast<const float2 *>(bs.live),
                             vw.channels, reinterpret_cast<const float4 *>(bs.nodes), bs.root_box, bs.n};
         const HitSink hs{nullptr, nullptr, 0};
         f3 ro = mk3(vw.origin[0], vw.origin[1], vw.origin[2]);
@@ -912,7 +1032,8 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
         }
         __syncwarp();
         RayResult r;
-        trace_ray<KB>(sc, k, ro, rd, inside, false, hs, status, kbuf, r, &sfr[warp], sstk[warp], scand[warp]);
+        trace_ray<KB>(sc, k, ro, rd, inside, false, hs, status, kbuf, r, &sfr[warp], sstk[warp], scand[warp],
+                      &scc[warp]);
         if (!inside) continue;
         float r0, r1, r2;
         finish_ray(r, bs.bg, 1e-12f, false, r0, r1, r2);
@@ -947,6 +1068,7 @@ static FwdArgs forward_args(const gray_params &p, bool display) {
     a.grads_enabled = p.metadata.grads_enabled;
     a.total_num_calls = p.metadata.total_num_calls;
     a.geom = reinterpret_cast<const float4 *>(p.scene.geom);
+    a.l2w = reinterpret_cast<const float4 *>(p.scene.l2w);
     a.live = reinterpret_cast<const float2 *>(p.scene.live);
     a.channels = p.gaussians.channels;
     a.nodes = reinterpret_cast<const float4 *>(p.scene.nodes);
@@ -989,9 +1111,9 @@ cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_
     dim3 grid((p.render_width + bw - 1) / bw, (p.render_height + bh - 1) / bh);
     switch (v & 3) {
         case 0: trace_forward_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(a); break;
-        case 1: trace_forward_kernel<32, 6><<<grid, kFwdThreads, 0, s>>>(a); break;
+        case 1: trace_forward_kernel<32, 4><<<grid, kFwdThreads, 0, s>>>(a); break;
         case 2: trace_forward_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(a); break;
-        default: trace_forward_kernel<16, 8><<<grid, kFwdThreads, 0, s>>>(a); break;
+        default: trace_forward_kernel<16, 7><<<grid, kFwdThreads, 0, s>>>(a); break;
     }
     return cudaGetLastError();
 }
@@ -1009,9 +1131,9 @@ cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_
     if ((e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
     switch (v & 3) {
         case 0: trace_batch_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
-        case 1: trace_batch_kernel<32, 6><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
+        case 1: trace_batch_kernel<32, 4><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
         case 2: trace_batch_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
-        default: trace_batch_kernel<16, 8><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
+        default: trace_batch_kernel<16, 7><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
     }
     return cudaGetLastError();
 }

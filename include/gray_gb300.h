@@ -129,7 +129,7 @@ typedef struct gray_hitlist {
 /* Scene-side workspace owned by the caller (sizes from gray_scene_workspace_sizes). */
 typedef struct gray_scene {
     float *geom;        /* [N,12] snapshot rows (M | mu), M = diag(1/s) R^T          */
-    float *l2w;         /* [N,12] snapshot rows of R diag(s)                          */
+    float *l2w;         /* [N,12] snapshot rows (L | mu), L = R diag(s)               */
     float *aabb;        /* [N,8]  leaf boxes (min xyz, pad, max xyz, pad)             */
     uint8_t *visible;   /* [N]    snapshot visibility (populate_bvh_kernel mask)      */
     float *live;        /* [N,2]  per-forward (sigmoid(opacity), scaling factor)      */
@@ -174,6 +174,7 @@ typedef struct gray_params {
  * gray_forward_pass_display of the same view. */
 typedef struct gray_batch_scene {
     const float *geom, *live, *nodes, *root_box; /* a scene's gray_scene buffers after rebuild/update */
+    const float *l2w;                            /* its gray_scene.l2w (may be NULL: no leaf culling) */
     int32_t n;                                   /* Gaussian count */
     float exp_power, alpha_threshold, t_threshold;
     float bg[3];

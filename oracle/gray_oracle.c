@@ -236,7 +236,7 @@ void orc_snapshot(int n, const float *mean, const float *rotation, const float *
                 L[4 * r + c] = R[3 * r + c] * s[c];
             }
             g[4 * r + 3] = mu[r];
-            L[4 * r + 3] = 0.0f;
+            L[4 * r + 3] = mu[r];
         }
         float *b = aabb + 8 * i;
         if (vis) {
