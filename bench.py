@@ -38,7 +38,7 @@ LR = dict(mean=1.6e-4, scale=5e-3, rotation=1e-3, opacity=2.5e-2, sh=2.5e-3)
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-gaussians", type=int, default=3_000_000)
@@ -75,24 +75,48 @@ def make_camera(a, rank):
 # GPU arm
 # ----------------------------------------------------------------------------------------------
 class ClockSampler:
-    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
-             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
-             "clocks_event_reasons.sw_power_cap"
+    """nvidia-smi clock / throttle-reason samples every 20 ms; stop() keeps the samples whose
+    timestamps fall inside the marked window (mark_begin .. mark_end)."""
+    FIELDS = "timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active," \
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
 
     def __init__(self, gpu_index):
         self.proc = None
         self.gpu = gpu_index
         self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
+            # wait (at most 3 s) until sampling has begun
+            deadline = time.time() + 3.0
+            while time.time() < deadline and os.path.getsize(self.path) == 0:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
+
+    def mark_begin(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
+
+    @staticmethod
+    def _epoch(stamp):
+        from datetime import datetime
+
+        for fmt in ("%Y/%m/%d %H:%M:%S.%f", "%Y/%m/%d %H:%M:%S"):
+            try:
+                return datetime.strptime(stamp.strip(), fmt).timestamp()
+            except ValueError:
+                pass
+        return None
 
     def stop(self):
         if self.proc is None:
@@ -106,14 +130,18 @@ class ClockSampler:
         rows = []
         for line in open(self.path):
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
+            if len(parts) >= 10:
                 rows.append(parts)
+        if self.t0 is not None and self.t1 is not None:
+            inside = [r for r in rows if (lambda t: t is not None and self.t0 - 0.05 <= t <= self.t1 + 0.05)(
+                self._epoch(r[0]))]
+            rows = inside or rows[-1:]
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        sm = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        mx = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[6 + i].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
 
@@ -210,8 +238,10 @@ def gpu_arm(a, rank, world, local_rank):
     st.reset()
     clocks = ClockSampler(local_rank)
     clocks.start()
+    clocks.mark_begin()
     with _lib.Profiler(capacity=64 * (a.steps + 1)) as prof:
         ms = timed(lambda: train_step(target_dev), a.steps)
+    clocks.mark_end()
     clk = clocks.stop()
     rt.cuda_module.check_status()
     H = float(st.num_gaussians_hit.sum().item()) / a.steps

@@ -37,13 +37,15 @@ struct AdamArgs {
 
 __global__ void step_count_kernel(uint32_t *total_num_steps) { *total_num_steps += 1u; }
 
+// ibc1 / ibc2 = 1 / (1 - beta^(step+1)): the bias corrections as multiplications, leaving one
+// division and one square root per element (the kernel is otherwise issue-bound on GB300).
 __device__ __forceinline__ void adam_one(float &p, float &m, float &v, float &g, float lr, float b1, float b2,
-                                         float bc1, float bc2, float eps, bool zero) {
+                                         float ibc1, float ibc2, float eps, bool zero) {
     const float gg = g;
     m = b1 * m + (1.0f - b1) * gg;
     v = b2 * v + (1.0f - b2) * gg * gg;
-    const float mh = m / bc1;
-    const float vh = v / bc2;
+    const float mh = m * ibc1;
+    const float vh = v * ibc2;
     p = p - lr * mh / (sqrtf(vh) + eps);
     if (zero) g = gg * 0.0f;
 }
@@ -66,8 +68,8 @@ __global__ void __launch_bounds__(kAdamThreads) adam_kernel(const AdamArgs a) {
         do_adam = false;
     }
     if (threadIdx.x == 0) {
-        s_bc[0] = 1.0f - adam_pow(b1, step + 1);
-        s_bc[1] = 1.0f - adam_pow(b2, step + 1);
+        s_bc[0] = 1.0f / (1.0f - adam_pow(b1, step + 1));
+        s_bc[1] = 1.0f / (1.0f - adam_pow(b2, step + 1));
     }
     __syncthreads();
     const float bc1 = s_bc[0], bc2 = s_bc[1];

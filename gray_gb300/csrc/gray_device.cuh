@@ -247,6 +247,15 @@ __device__ __forceinline__ bool intersect_hits(const float4 g0, const float4 g1,
     return true;
 }
 
+// Colour in 2^-24 fixed point (clamped to [-64, 64], so it fits 31 bits): the tail sums add
+// alpha16_fixed(a) * colour_fixed(c), an exact 64-bit product in 2^-48 units.
+__device__ __forceinline__ int colour_fixed(float c) {
+    return (int)to_fixed(fminf(fmaxf(c, -64.0f), 64.0f), 0x1.0p24f);
+}
+__device__ __forceinline__ long long mul_fixed(long long a16fix, int cfix) {
+    return (long long)(int)a16fix * (long long)cfix;
+}
+
 // alpha * 2^24 for an fp16 alpha in [0, 1): an exact integer, from the half's bits
 __device__ __forceinline__ long long alpha16_fixed(uint16_t a16) {
     const uint32_t e = (a16 >> 10) & 0x1fu, m = a16 & 0x3ffu;

@@ -141,19 +141,19 @@ struct RayResult {
 // live values and colour the caller has fetched.
 template <int KB>
 __device__ __forceinline__ void on_leaf_data(uint32_t gid, const float4 g0, const float4 g1, const float4 g2,
-                                             const float2 lv, float c0, float c1, float c2, bool first, f3 ro,
-                                             f3 rd, const TraceKnobs &k, LaneState &st,
+                                             const float2 lv, int cf0, int cf1, int cf2, bool first, f3 ro, f3 rd,
+                                             const TraceKnobs &k, LaneState &st,
                                              unsigned long long (*kbuf)[kFwdThreads]) {
     float dist, alpha;
     if (!intersect(g0, g1, g2, lv.x, lv.y, ro, rd, k.athr, k.pw, k.znear, k.zfar, dist, alpha)) return;
     const uint16_t a16 = f2h_bits(alpha), d16 = f2h_bits(dist);
     if (first) {
         add_log_transmittance(st.lfx, alpha);
-        const float af = h2f_bits(a16);
-        st.afx += alpha16_fixed(a16);
-        st.cfx0 += to_fixed(af * c0, 0x1.0p32f);
-        st.cfx1 += to_fixed(af * c1, 0x1.0p32f);
-        st.cfx2 += to_fixed(af * c2, 0x1.0p32f);
+        const long long a = alpha16_fixed(a16);
+        st.afx += a;
+        st.cfx0 += mul_fixed(a, cf0);
+        st.cfx1 += mul_fixed(a, cf1);
+        st.cfx2 += mul_fixed(a, cf2);
         st.nhit++;
     }
     if (!(h2f_bits(d16) > k.znear)) return;
@@ -188,14 +188,15 @@ __device__ __forceinline__ void on_leaf(const TraceScene &sc, uint32_t gid, bool
     const float4 g0 = sc.geom[3 * gid], g1 = sc.geom[3 * gid + 1], g2 = sc.geom[3 * gid + 2];
     const float2 lv = sc.live[gid];
     const float *cp = sc.channels + 3 * (size_t)gid;
-    on_leaf_data<KB>(gid, g0, g1, g2, lv, cp[0], cp[1], cp[2], first, ro, rd, k, st, kbuf);
+    on_leaf_data<KB>(gid, g0, g1, g2, lv, colour_fixed(cp[0]), colour_fixed(cp[1]), colour_fixed(cp[2]), first, ro,
+                     rd, k, st, kbuf);
 }
 
 // Per-warp shared-memory copy of the queued leaves' records, filled once per flush by the lanes
 // (one candidate each, all loads in flight together) and read by every lane afterwards.
 struct CandCache {
     float4 g[kCand][3];  // snapshot rows (M | mu)
-    float4 c[kCand];     // colour, live opacity
+    int4 c[kCand];       // colour in 2^-24 fixed point (x, y, z), live opacity bits (w)
     float sf[kCand];     // live scaling factor
 };
 
@@ -297,7 +298,8 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     uint32_t gid = 0;
     bool keep = false;
-    float4 g0, g1, g2, cv;
+    float4 g0, g1, g2;
+    int4 cv;
     float sfv = 0.0f;
     if (lane < nc) {
         gid = cand[lane];
@@ -306,7 +308,7 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
         g2 = sc.geom[3 * (size_t)gid + 2];
         const float2 lv = sc.live[gid];
         const float *cp = sc.channels + 3 * (size_t)gid;
-        cv = make_float4(cp[0], cp[1], cp[2], lv.x);
+        cv = make_int4(colour_fixed(cp[0]), colour_fixed(cp[1]), colour_fixed(cp[2]), __float_as_int(lv.x));
         sfv = lv.y;
         keep = sc.l2w ? frustum_ellipsoid(fr, sc.l2w + 3 * (size_t)gid) : true;
     }
@@ -326,7 +328,8 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
     uint32_t mask = 0u;
     if (want) {
         for (int j = 0; j < nc; j++) {
-            if (intersect_hits(cc.g[j][0], cc.g[j][1], cc.g[j][2], cc.c[j].w, ro, rd, k.athr, k.znear, k.zfar))
+            if (intersect_hits(cc.g[j][0], cc.g[j][1], cc.g[j][2], __int_as_float(cc.c[j].w), ro, rd, k.athr,
+                               k.znear, k.zfar))
                 mask |= 1u << j;
         }
     }
@@ -334,9 +337,9 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
         if (mask != 0u) {
             const int j = __ffs(mask) - 1;
             mask &= mask - 1u;
-            const float4 c = cc.c[j];
-            on_leaf_data<KB>(cand[j], cc.g[j][0], cc.g[j][1], cc.g[j][2], make_float2(c.w, cc.sf[j]), c.x, c.y,
-                             c.z, first, ro, rd, k, st, kbuf);
+            const int4 c = cc.c[j];
+            on_leaf_data<KB>(cand[j], cc.g[j][0], cc.g[j][1], cc.g[j][2], make_float2(__int_as_float(c.w), cc.sf[j]),
+                             c.x, c.y, c.z, first, ro, rd, k, st, kbuf);
         }
     }
     __syncwarp();
@@ -586,10 +589,11 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
                 const float al = h2f_bits((uint16_t)(key & 0xFFFFu));
                 const float *c = sc.channels + 3 * (size_t)gid;
                 const float cx = c[0], cy = c[1], cz = c[2];
-                st.afx -= alpha16_fixed((uint16_t)(key & 0xFFFFu));
-                st.cfx0 -= to_fixed(al * cx, 0x1.0p32f);
-                st.cfx1 -= to_fixed(al * cy, 0x1.0p32f);
-                st.cfx2 -= to_fixed(al * cz, 0x1.0p32f);
+                const long long a = alpha16_fixed((uint16_t)(key & 0xFFFFu));
+                st.afx -= a;
+                st.cfx0 -= mul_fixed(a, colour_fixed(cx));
+                st.cfx1 -= mul_fixed(a, colour_fixed(cy));
+                st.cfx2 -= mul_fixed(a, colour_fixed(cz));
                 const float w = T * al;
                 C0 = C0 + cx * w;
                 C1 = C1 + cy * w;
@@ -674,9 +678,9 @@ __device__ __forceinline__ void finish_ray(RayResult &r, const float *bg, float 
     r0 = r1 = r2 = 0.0f;
     if (st.afx > 0) {
         const float sa = __ll2float_rn(st.afx) * 0x1.0p-24f;
-        r0 = (__ll2float_rn(st.cfx0) * 0x1.0p-32f) / sa;
-        r1 = (__ll2float_rn(st.cfx1) * 0x1.0p-32f) / sa;
-        r2 = (__ll2float_rn(st.cfx2) * 0x1.0p-32f) / sa;
+        r0 = (__ll2float_rn(st.cfx0) * 0x1.0p-48f) / sa;
+        r1 = (__ll2float_rn(st.cfx1) * 0x1.0p-48f) / sa;
+        r2 = (__ll2float_rn(st.cfx2) * 0x1.0p-48f) / sa;
     }
     r.C0 = r.C0 + rT * r0;
     r.C1 = r.C1 + rT * r1;

@@ -17,7 +17,8 @@
  *   cuda/opt/adam.cu:6-83             fused Adam
  * Deliberate, documented differences from the reference (shared with the CUDA path):
  *   - the all-hit "skipped" sums (forward_pass.cu:50-56, 92-93) are accumulated exactly in
- *     64-bit fixed point instead of an order-dependent fp32 running sum;
+ *     64-bit fixed point (alpha16 in 2^-24 units times the colour in 2^-24 units, clamped to
+ *     [-64, 64]) instead of an order-dependent fp32 running sum;
  *   - the full transmittance (shaders.cu:55-56, an fp32 product in traversal order) is the
  *     exponential of a fixed-point sum of log(1 - alpha), so it does not depend on the order;
  *   - hits with equal fp16 distance are ordered by gaussian id (the reference uses OptiX
@@ -685,14 +686,20 @@ static inline void add_log_transmittance(int64_t *s, float alpha) {
 }
 static inline float full_transmittance(int64_t s) { return orc_expf((float)s * 0x1.0p-40f); }
 
+/* colour in 2^-24 fixed point, clamped to [-64, 64]; a tail-sum term is alpha16 (2^-24 units) times
+ * this, an exact 64-bit product in 2^-48 units */
+static inline int32_t colour_fixed(float c) { return (int32_t)to_fixed(fminf(fmaxf(c, -64.0f), 64.0f), 0x1.0p24f); }
+static inline int64_t mul_fixed(int64_t a16fix, int32_t cfix) { return (int64_t)(int32_t)a16fix * (int64_t)cfix; }
+
 static inline void record_hit(hit_acc *acc, ray_scratch *scr, uint32_t gid, is_result h, const float *channels,
                               float znear) {
     add_log_transmittance(&acc->lfx, h.alpha);
     uint16_t a16 = orc_f2h(h.alpha), d16 = orc_f2h(h.dist);
     float af = orc_h2f(a16);
     const float *c = channels + 3 * (size_t)gid;
-    acc->afx += to_fixed(af, 0x1.0p24f);
-    for (int k = 0; k < 3; k++) acc->cfx[k] += to_fixed(af * c[k], 0x1.0p32f);
+    const int64_t a = to_fixed(af, 0x1.0p24f);
+    acc->afx += a;
+    for (int k = 0; k < 3; k++) acc->cfx[k] += mul_fixed(a, colour_fixed(c[k]));
     acc->nhit++;
     if (orc_h2f(d16) > znear) push_key(scr, ((uint64_t)d16 << 48) | ((uint64_t)gid << 16) | a16);
 }
@@ -808,8 +815,9 @@ static void trace_one(fwd_job *J, int r, ray_scratch *scr) {
         uint32_t gid = (uint32_t)(key >> 16);
         float a = orc_h2f((uint16_t)(key & 0xffffu));
         const float *c = J->channels + 3 * (size_t)gid;
-        acc.afx -= to_fixed(a, 0x1.0p24f);
-        for (int k = 0; k < 3; k++) acc.cfx[k] -= to_fixed(a * c[k], 0x1.0p32f);
+        const int64_t afix = to_fixed(a, 0x1.0p24f);
+        acc.afx -= afix;
+        for (int k = 0; k < 3; k++) acc.cfx[k] -= mul_fixed(afix, colour_fixed(c[k]));
         float w = T * a;
         for (int k = 0; k < 3; k++) C[k] = C[k] + c[k] * w;
         if (cfg->render_depth) depth = depth + d * w;
@@ -823,7 +831,7 @@ static void trace_one(fwd_job *J, int r, ray_scratch *scr) {
     float rem[3] = {0.0f, 0.0f, 0.0f};
     if (acc.afx > 0) {
         float sa = (float)acc.afx * 0x1.0p-24f;
-        for (int k = 0; k < 3; k++) rem[k] = ((float)acc.cfx[k] * 0x1.0p-32f) / sa;
+        for (int k = 0; k < 3; k++) rem[k] = ((float)acc.cfx[k] * 0x1.0p-48f) / sa;
     }
     for (int k = 0; k < 3; k++) C[k] = C[k] + rT * rem[k];
     if (cfg->render_depth) depth = depth / fmaxf(1.0f - T, cfg->eps_forward_normalization);
@@ -1055,7 +1063,7 @@ void orc_trace_backward(int nrays, int launch_w, int launch_h, const float *ray_
 /* fused Adam: cuda/opt/adam.cu:6-83                                                           */
 /* ------------------------------------------------------------------------------------------ */
 typedef struct {
-    float b1, b2, eps, bc1, bc2;
+    float b1, b2, eps, ibc1, ibc2; /* ibc = 1 / (1 - beta^(step+1)) */
     int zero;
 } adam_k;
 
@@ -1063,8 +1071,8 @@ static inline void adam_el(const adam_k *a, float *p, float *m, float *v, float 
     float gg = *g;
     float mm = a->b1 * *m + (1.0f - a->b1) * gg;
     float vv = a->b2 * *v + (1.0f - a->b2) * gg * gg;
-    float mh = mm / a->bc1;
-    float vh = vv / a->bc2;
+    float mh = mm * a->ibc1;
+    float vh = vv * a->ibc2;
     *p = *p - lr * mh / (sqrtf(vh) + a->eps);
     *m = mm;
     *v = vv;
@@ -1073,8 +1081,8 @@ static inline void adam_el(const adam_k *a, float *p, float *m, float *v, float 
 
 void orc_adam_step(orc_adam_state *s, int step, int zero_grads, int update_channels, float beta1, float beta2,
                    float eps, int enable_sh, int laziness) {
-    adam_k a = {beta1, beta2, eps, 1.0f - orc_adam_pow(beta1, step + 1), 1.0f - orc_adam_pow(beta2, step + 1),
-                zero_grads};
+    adam_k a = {beta1, beta2, eps, 1.0f / (1.0f - orc_adam_pow(beta1, step + 1)),
+                1.0f / (1.0f - orc_adam_pow(beta2, step + 1)), zero_grads};
     for (int i = 0; i < s->n; i++) {
         for (int k = 0; k < 3; k++) {
             size_t j = 3 * (size_t)i + k;
