@@ -59,12 +59,12 @@ def _check(L, rc, what):
 
 
 # untuned choice: 4x8 packets with a 16-entry k-buffer (the library's default variant), as many
-# blocks per SM as its shared memory and register cap allow (7)
-DEFAULT_VARIANT, DEFAULT_BLOCKS_PER_SM = 7, 7
+# blocks per SM as its register cap allows (6)
+DEFAULT_VARIANT, DEFAULT_BLOCKS_PER_SM = 7, 6
 # candidates the autotuner tries: (kernel variant, persistent blocks per SM), each variant with the
 # block counts around its residency limit (32-entry buffers: 4 per SM; 16 entries uncapped: 3;
-# 16 entries capped: 7)
-TUNE_CANDIDATES = [(1, 4), (5, 4), (2, 3), (6, 3), (3, 6), (3, 7), (7, 6), (7, 7)]
+# 16 entries capped: 6)
+TUNE_CANDIDATES = [(1, 4), (5, 4), (2, 3), (6, 3), (3, 5), (3, 6), (7, 5), (7, 6)]
 
 
 @dataclass

@@ -9,7 +9,7 @@
 namespace gray {
 
 // forward-kernel variant used when gray_params.trace_variant (or a batch launch's variant) is 0:
-// 4x8 packets, 16-entry k-buffer, 7 blocks per SM
+// 4x8 packets, 16-entry k-buffer, 6 blocks per SM
 constexpr int kDefaultTraceVariant = 7;
 
 // scene.cu

@@ -1117,7 +1117,7 @@ cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_
         case 0: trace_forward_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(a); break;
         case 1: trace_forward_kernel<32, 4><<<grid, kFwdThreads, 0, s>>>(a); break;
         case 2: trace_forward_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(a); break;
-        default: trace_forward_kernel<16, 7><<<grid, kFwdThreads, 0, s>>>(a); break;
+        default: trace_forward_kernel<16, 6><<<grid, kFwdThreads, 0, s>>>(a); break;
     }
     return cudaGetLastError();
 }
@@ -1137,7 +1137,7 @@ cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_
         case 0: trace_batch_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
         case 1: trace_batch_kernel<32, 4><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
         case 2: trace_batch_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
-        default: trace_batch_kernel<16, 7><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
+        default: trace_batch_kernel<16, 6><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
     }
     return cudaGetLastError();
 }
