@@ -253,6 +253,15 @@ __device__ __forceinline__ void store_child_box(float *nodes, int node, int slot
     for (int k = 0; k < 6; k++) __stcg(nd + k, b[k]);
 }
 
+// atomicAdd with acquire-release semantics at GPU scope: the child box stored before it is visible
+// to whichever thread observes the count after it, and that thread sees the sibling's box (the
+// release/acquire pair replaces two full fences).
+__device__ __forceinline__ uint32_t add_acq_rel(uint32_t *p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 __global__ void refit_kernel(int n, const float4 *__restrict__ aabb, const uint32_t *__restrict__ order,
                              const int32_t *__restrict__ leaf_parent, const int32_t *__restrict__ int_parent,
                              float *__restrict__ nodes, uint32_t *__restrict__ flags, float *__restrict__ root_box) {
@@ -277,9 +286,7 @@ __global__ void refit_kernel(int n, const float4 *__restrict__ aabb, const uint3
     for (int guard = 0; guard < 128; guard++) {
         uint32_t c0 = __float_as_uint(__ldcg(nodes + 16 * (size_t)p + 12));
         store_child_box(nodes, p, c0 == link ? 0 : 1, box);
-        __threadfence();
-        if (atomicAdd(&flags[p], 1u) == 0u) return;
-        __threadfence();
+        if (add_acq_rel(&flags[p], 1u) == 0u) return;
         const float *nd = nodes + 16 * (size_t)p;
         float u[6];
 #pragma unroll
