@@ -36,6 +36,10 @@ LR = dict(mean=1.6e-4, scale=5e-3, rotation=1e-3, opacity=2.5e-2, sh=2.5e-3)
 
 
 def parse():
+    return parse_args(None)
+
+
+def parse_args(argv):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=30)
@@ -49,7 +53,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and served measurements")
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--no-served", action="store_true", help="skip the served measurement only")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def workload_config(a, rank=0):
@@ -154,6 +158,23 @@ def measured_peak_gbs():
         return 6800.0, "fallback"
 
 
+def max_over_ranks(ms, world, device):
+    """The job's time is the slowest replica's: MAX all-reduce over the ranks (no-op for one rank)."""
+    if world <= 1:
+        return ms
+    import torch
+
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, ms, world):
+    """Units per second of all replicas together: every rank processes units_per_rank in the
+    (max-over-ranks) time ms (weak scaling)."""
+    return units_per_rank * world / (ms / 1000.0)
+
+
 def ncu_traffic(kernel, a):
     """DRAM bytes (read + write) of one launch of `kernel` on this workload, from an ncu capture
     summarised in profiles/ncu_traffic.json (key "<kernel> <gaussians> <width>x<height>")."""
@@ -221,12 +242,7 @@ def gpu_arm(a, rank, world, local_rank):
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(e0.elapsed_time(e1), world, dev)
 
     for _ in range(a.warmup):
         train_step(target_dev)
@@ -248,20 +264,20 @@ def gpu_arm(a, rank, world, local_rank):
     A = float(st.num_gaussians_accumulated.sum().item()) / a.steps
     R = a.width * a.height
     ms_step = ms / a.steps
-    steps_per_s = 1000.0 / ms_step * world
+    steps_per_s = whole_job_rate(a.steps, ms, world)
 
     # ---- e2e through the public API with host buffers ----
     for _ in range(max(1, a.warmup // 2)):
         e2e_step()
     ms_e2e = timed(e2e_step, a.steps)
-    e2e_steps_per_s = 1000.0 / (ms_e2e / a.steps) * world
+    e2e_steps_per_s = whole_job_rate(a.steps, ms_e2e, world)
 
     # ---- render-only throughput (inference-style forward, no grads) ----
     with torch.no_grad():
         for _ in range(2):
             rt(cam, skip_copy=True)
         ms_render = timed(lambda: rt(cam, skip_copy=True), a.steps)
-    rays_per_s = R * a.steps / (ms_render / 1000.0) * world
+    rays_per_s = whole_job_rate(R * a.steps, ms_render, world)
 
     # ---- roofline of the dominant kernel ----
     res = prof.results

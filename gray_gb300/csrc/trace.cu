@@ -465,16 +465,6 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
     bool done = !alive;
     uint32_t head = GRAY_NULL;
 
-    const SlabRay sr = make_slab_ray(ro, rd, 2.0e-6f * (fabsf(ro.x) + fabsf(ro.y) + fabsf(ro.z)));
-    // packet lead direction for the near/far child order (any deterministic choice is valid)
-    float lx = alive ? rd.x : 0.0f, ly = alive ? rd.y : 0.0f, lz = alive ? rd.z : 0.0f;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        lx += __shfl_xor_sync(kFull, lx, off);
-        ly += __shfl_xor_sync(kFull, ly, off);
-        lz += __shfl_xor_sync(kFull, lz, off);
-    }
-
     bool first = true;
     int traversals = 0;
     const int n = sc.n;
@@ -497,11 +487,22 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
         }
         if (!per_ray) {
         } else if (n == 1) {
+            // (the per-ray path's ray data is built here, so it holds no registers in the frustum path)
+            const SlabRay sr = make_slab_ray(ro, rd, 2.0e-6f * (fabsf(ro.x) + fabsf(ro.y) + fabsf(ro.z)));
             const float *rb = sc.root_box;
             const float bmin[3] = {rb[0], rb[1], rb[2]}, bmax[3] = {rb[4], rb[5], rb[6]};
             bool h = want && slab_hit(bmin, bmax, sr);
             if (__any_sync(kFull, h)) on_leaf<KB>(sc, 0u, h, first, ro, rd, k, st, kbuf);
         } else if (n > 1) {
+            const SlabRay sr = make_slab_ray(ro, rd, 2.0e-6f * (fabsf(ro.x) + fabsf(ro.y) + fabsf(ro.z)));
+            // packet lead direction for the near/far child order (any deterministic choice is valid)
+            float lx = alive ? rd.x : 0.0f, ly = alive ? rd.y : 0.0f, lz = alive ? rd.z : 0.0f;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                lx += __shfl_xor_sync(kFull, lx, off);
+                ly += __shfl_xor_sync(kFull, ly, off);
+                lz += __shfl_xor_sync(kFull, lz, off);
+            }
             uint32_t stk0 = 0, stk1 = 0;  // entry e lives in lane e%32, word e/32
             int sp = 0;
             {
