@@ -412,6 +412,7 @@ def served_form(a, rank):
     warm.drain()
     torch.cuda.synchronize()
     srv = RenderServer(tracers, slots=2, max_batch=16)
+    tuned = srv.tune([(s_, cam) for _, s_, cam in sched[:16]])
     reqs, wall = run_served(srv, sched)
     lat = np.array([r.latency for r in reqs]) * 1000.0
     rays = sum(r.rays for r in reqs)
@@ -422,7 +423,8 @@ def served_form(a, rank):
            "rays_per_s": round(rays / wall, 1),
            "plain_p50_ms": round(float(np.percentile(lat_p, 50)), 2),
            "plain_p99_ms": round(float(np.percentile(lat_p, 99)), 2),
-           "plain_rays_per_s": round(rays / wall_p, 1), "offered_rays_per_s": round(rays / sched[-1][0], 1)}
+           "plain_rays_per_s": round(rays / wall_p, 1), "offered_rays_per_s": round(rays / sched[-1][0], 1),
+           "tuned": list(tuned)}
     del tracers
     torch.cuda.empty_cache()
     return out

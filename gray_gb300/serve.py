@@ -73,6 +73,20 @@ class RenderServer:
         self.inflight_bytes = 0
         self._next = 0
 
+    def tune(self, sample):
+        """Pick the kernel variant and persistent grid size once, with the batch autotuner, on a
+        representative list of (scene, camera) requests; every later batch uses the choice (a
+        per-batch tuning would cost more than it saves, since served batches rarely repeat)."""
+        probe = BatchRenderer(self.tracers, use_graph=False, autotune=True, cache_plans=False)
+        reqs = sorted(((int(s), c) for s, c in sample), key=lambda r: r[0])
+        probe._scene_table()
+        choice = probe._tune(reqs)
+        torch.cuda.synchronize(self.device)
+        for sl in self.slots:
+            sl.renderer.fixed = choice
+            sl.renderer.tuned.clear()
+        return choice
+
     def submit(self, scene: int, camera: CameraInfo, arrival: float | None = None) -> Request:
         r = Request(self._next, scene, camera, time.perf_counter() if arrival is None else arrival)
         self._next += 1

@@ -55,3 +55,25 @@ def test_served_results_equal_alone_and_in_mix():
         ref = tracers[s].get_framebuffer().output_channels[:h, :w].permute(2, 0, 1)
         got = next(r.image for r in reqs if r.camera is cam)
         assert torch.equal(got, ref)
+
+
+def test_tuned_server_renders_the_same_pixels():
+    """A server whose kernel variant was picked once by the autotuner renders exactly what the
+    untuned server renders (every variant gives the same pixels)."""
+    tracers = [_scene_tracer(40_000, 1, 160, 120), _scene_tracer(90_000, 2, 160, 120)]
+    cams = [(0, synthetic.orbit_camera(0.5, 160, 120)), (1, synthetic.orbit_camera(2.0, 96, 96)),
+            (0, synthetic.orbit_camera(4.0, 64, 48))]
+    tuned = RenderServer(tracers, slots=2, reserve_bytes=0, keep_images=True)
+    choice = tuned.tune(cams)
+    assert len(choice) == 2
+    plain = RenderServer(tracers, slots=1, reserve_bytes=0, keep_images=True)
+    for s, cam in cams:
+        tuned.submit(s, cam)
+        plain.submit(s, cam)
+    tuned.drain()
+    plain.drain()
+    torch.cuda.synchronize()
+    a = sorted(tuned.completed, key=lambda r: r.rid)
+    b = sorted(plain.completed, key=lambda r: r.rid)
+    for x, y in zip(a, b):
+        assert torch.equal(x.image, y.image)
