@@ -58,7 +58,7 @@ class StatsC(ctypes.Structure):
 
 
 class HitlistC(ctypes.Structure):
-    _fields_ = _ptrs("head_per_pixel", "total_words", "pool") + [("size", ctypes.c_uint32)]
+    _fields_ = _ptrs("head_per_pixel", "total_words", "pool") + [("size", ctypes.c_uint32)] + _ptrs("schedule")
 
 
 class SceneC(ctypes.Structure):
@@ -102,6 +102,8 @@ def load(path: str | None = None):
         f.argtypes = [ctypes.POINTER(ParamsC), ctypes.c_void_p]
     L.gray_sort_tmp_words.restype = ctypes.c_size_t
     L.gray_sort_tmp_words.argtypes = [ctypes.c_int32]
+    L.gray_schedule_words.restype = ctypes.c_size_t
+    L.gray_schedule_words.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
     L.gray_profiler_enable.restype = ctypes.c_int
     L.gray_profiler_enable.argtypes = [ctypes.c_int, ctypes.c_int]
     L.gray_profiler_collect.restype = ctypes.c_int

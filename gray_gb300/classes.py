@@ -328,6 +328,9 @@ class Raytracer:
         self.ppll_backward_data = PPLLDataHolder("backward", self.width, self.height,
                                                  1 if inference_only else ppll_backward_size, dev)
         self.status = torch.zeros(1, device=dev, dtype=torch.int32)
+        # work order of the forward's pixel tiles (densest first), rebuilt by every forward
+        self.schedule = torch.zeros(int(_lib.load().gray_schedule_words(self.width, self.height)), device=dev,
+                                    dtype=torch.int32)
         self.trace_variant = 0  # forward-kernel variant (0 = library default); results do not depend on it
         self._scene = _SceneWorkspace(1, dev, not self.inference_only)
         self._params = None
@@ -361,6 +364,7 @@ class Raytracer:
         p.hitlist.total_words = _p(h.total_hits)
         p.hitlist.pool = _p(h.pool)
         p.hitlist.size = h.size
+        p.hitlist.schedule = _p(self.schedule)
         p.scene = self._scene.struct()
         p.status = _p(self.status)
         p.trace_variant = int(self.trace_variant)

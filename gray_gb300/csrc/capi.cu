@@ -149,6 +149,8 @@ int gray_profiler_collect(char *buf, size_t buflen) {
 
 size_t gray_sort_tmp_words(int32_t n) { return gray::sort_tmp_words(n); }
 
+size_t gray_schedule_words(uint32_t width, uint32_t height) { return gray::gray_schedule_words_for(width, height); }
+
 int gray_forward_pass(const gray_params *p, void *stream) {
     int e = check_trace(p);
     if (e) return e;

@@ -28,6 +28,7 @@ size_t sort_tmp_words(int n);
 // trace.cu
 // display: forward_pass_display (colour only; no hit lists or saved state, whatever grads_enabled holds)
 cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_t s);
+size_t gray_schedule_words_for(uint32_t width, uint32_t height);
 // ellipsoid view; a no-op launch unless config.render_ellipsoids is set
 cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s);
 cudaError_t launch_trace_backward(const gray_params &p, cudaStream_t s);

@@ -32,6 +32,7 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWideStack = 256;  // per-warp shared stack of the frustum traversal
 constexpr int kCand = 32;        // leaves processed per flush (one per lane)
 constexpr int kQueue = 3 * kCand; // per-warp queue of leaves: < kCand before a step, + up to 64 per step
+constexpr int kSchedHeader = 64;  // schedule words before the per-tile estimates
 
 struct FwdArgs {
     uint32_t alloc_w, render_w, render_h;
@@ -43,6 +44,8 @@ struct FwdArgs {
     const uint8_t *render_ellipsoids;
     const float *ellipsoid_min_opacity;
     int display;  // forward_pass_display: colour only, whatever grads_enabled holds
+    uint32_t *schedule;  // work order of the pixel tiles (null: tiles in launch order)
+    int tiles_x, ntiles;
     const uint32_t *total_num_calls;
     const float4 *geom, *l2w;
     const float2 *live;
@@ -705,17 +708,24 @@ __device__ __forceinline__ f3 camera_ray(const float *w, float fov, int px, int 
     return mk3(v.x * inv, v.y * inv, v.z * inv);
 }
 
-template <int KB, int MINB>
-__global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const FwdArgs a) {
-    __shared__ unsigned long long kbuf[KB][kFwdThreads];
-    __shared__ Frustum sfr[kWarps];
-    __shared__ uint32_t sstk[kWarps][kWideStack];
-    __shared__ uint32_t scand[kWarps][kQueue];
-    __shared__ CandCache scc[kWarps];
-    if (*a.render_ellipsoids) return;  // the ellipsoid view (ellipsoid_kernel) renders this frame
+// Shared memory of a forward block.
+template <int KB>
+struct FwdShared {
+    unsigned long long kbuf[KB][kFwdThreads];
+    Frustum sfr[kWarps];
+    uint32_t sstk[kWarps][kWideStack];
+    uint32_t scand[kWarps][kQueue];
+    CandCache scc[kWarps];
+};
+
+// One block's pixel tile (bx, by): 2x2 packets of tile_w x tile_h pixels, one per warp.
+template <int KB>
+__device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, FwdShared<KB> &sh) {
+    unsigned long long(*kbuf)[kFwdThreads] = sh.kbuf;
+    Frustum *sfr = sh.sfr;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int px = blockIdx.x * (a.tile_w * kBlockWarpsX) + (warp % kBlockWarpsX) * a.tile_w + (lane % a.tile_w);
-    const int py = blockIdx.y * (a.tile_h * kBlockWarpsY) + (warp / kBlockWarpsX) * a.tile_h + (lane / a.tile_w);
+    const int px = bx * (a.tile_w * kBlockWarpsX) + (warp % kBlockWarpsX) * a.tile_w + (lane % a.tile_w);
+    const int py = by * (a.tile_h * kBlockWarpsY) + (warp / kBlockWarpsX) * a.tile_h + (lane / a.tile_w);
     const bool inside = px < (int)a.render_w && py < (int)a.render_h;
     const uint32_t pixel = (uint32_t)py * a.alloc_w + (uint32_t)px;
 
@@ -766,8 +776,8 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const 
         __syncwarp();
     }
     RayResult r;
-    trace_ray<KB>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sstk[warp],
-                  scand[warp], &scc[warp]);
+    trace_ray<KB>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sh.sstk[warp],
+                  sh.scand[warp], &sh.scc[warp]);
 
     if (!inside) return;
     if (!alive) {
@@ -805,6 +815,127 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const 
         }
         a.head[pixel] = GRAY_NULL;
     }
+}
+
+// Grid launch: block (x, y) renders tile (x, y).
+template <int KB, int MINB>
+__global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const FwdArgs a) {
+    __shared__ FwdShared<KB> sh;
+    if (*a.render_ellipsoids) return;  // the ellipsoid view (ellipsoid_kernel) renders this frame
+    forward_tile<KB>(a, blockIdx.x, blockIdx.y, sh);
+}
+
+// Persistent launch: the blocks take tiles from the schedule's order, densest first, until none is
+// left (a separate kernel, so the grid launch keeps its register allocation).
+template <int KB, int MINB>
+__global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_sched_kernel(const FwdArgs a) {
+    __shared__ FwdShared<KB> sh;
+    __shared__ uint32_t s_next;
+    if (*a.render_ellipsoids) return;
+    for (;;) {
+        __syncthreads();  // every thread is done with the previous tile (and s_next)
+        if (threadIdx.x == 0) s_next = atomicAdd(a.schedule, 1u);
+        __syncthreads();
+        const uint32_t t = s_next;
+        if (t >= (uint32_t)a.ntiles) break;
+        const uint32_t tile = a.schedule[kSchedHeader + a.ntiles + t];
+        forward_tile<KB>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x), sh);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Work order of the forward's tiles.  A tile's work follows the number of Gaussians its rays meet
+// (per-packet time correlates 0.92 with hits), so the estimate is the number of leaves under the
+// BVH nodes its frustum reaches, cut where a node holds at most kCostCut leaves.  Tiles are then
+// counting-sorted by log2 of the estimate, largest first, so the launch does not end with a dense
+// tile started late.  Schedule words: [0] work counter, [1..33] bucket counts/cursors,
+// [kSchedHeader, +ntiles) estimates, [kSchedHeader + ntiles, +ntiles) order.
+// ---------------------------------------------------------------------------------------------
+constexpr int kCostCut = 512;
+constexpr int kCostStack = 256;
+
+__global__ void __launch_bounds__(32) tile_cost_kernel(const FwdArgs a, int bw, int bh) {
+    __shared__ Frustum fr;
+    __shared__ uint32_t stk[kCostStack];
+    const int tile = blockIdx.x, lane = threadIdx.x;
+    const uint32_t lanemask_lt = (1u << lane) - 1u;
+    uint32_t est = 0;
+    const int n = a.n;
+    if (!*a.rays_from_python && !*a.jitter && !*a.render_ellipsoids && n > 1) {
+        const int x0 = (tile % a.tiles_x) * bw, y0 = (tile / a.tiles_x) * bh;
+        const int x1 = min(x0 + bw, (int)a.render_w) - 1, y1 = min(y0 + bh, (int)a.render_h) - 1;
+        if (lane == 0) {
+            const f3 o = mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]);
+            const f3 d[4] = {camera_ray(a.w2c, *a.fov, x0, y0, a.render_w, a.render_h, 0.0f, 0.0f),
+                             camera_ray(a.w2c, *a.fov, x1, y0, a.render_w, a.render_h, 0.0f, 0.0f),
+                             camera_ray(a.w2c, *a.fov, x1, y1, a.render_w, a.render_h, 0.0f, 0.0f),
+                             camera_ray(a.w2c, *a.fov, x0, y1, a.render_w, a.render_h, 0.0f, 0.0f)};
+            make_frustum(fr, o, d);
+            stk[0] = 0u;
+        }
+        __syncwarp();
+        int sp = 1;
+        for (int guard = 0; sp > 0 && guard < 4096; guard++) {
+            const int take = sp < 32 ? sp : 32;
+            uint32_t node = GRAY_NULL;
+            if (lane < take) node = stk[sp - 1 - lane];
+            __syncwarp();
+            sp -= take;
+            uint32_t push[2] = {GRAY_NULL, GRAY_NULL};
+            if (node != GRAY_NULL && node < (uint32_t)(n - 1)) {
+                const float4 q0 = a.nodes[4 * node], q1 = a.nodes[4 * node + 1], q2 = a.nodes[4 * node + 2],
+                             q3 = a.nodes[4 * node + 3];
+                const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
+                const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
+                const uint32_t c[2] = {__float_as_uint(q3.x), __float_as_uint(q3.y)};
+                const bool in[2] = {frustum_box(fr, b0min, b0max), frustum_box(fr, b1min, b1max)};
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    if (!in[q]) continue;
+                    if (c[q] & GRAY_LEAF_BIT) {
+                        est += 1u;
+                    } else if (c[q] < (uint32_t)(n - 1)) {
+                        const uint32_t leaves = __float_as_uint(a.nodes[4 * c[q] + 3].z);
+                        if (leaves <= (uint32_t)kCostCut) est += leaves;
+                        else push[q] = c[q];
+                    }
+                }
+            }
+            const uint32_t m0 = __ballot_sync(kFull, push[0] != GRAY_NULL), m1 = __ballot_sync(kFull, push[1] != GRAY_NULL);
+            const int n0 = __popc(m0), n1 = __popc(m1);
+            if (sp + n0 + n1 > kCostStack) break;  // an estimate from what was reached is enough
+            if (push[0] != GRAY_NULL) stk[sp + __popc(m0 & lanemask_lt)] = push[0];
+            if (push[1] != GRAY_NULL) stk[sp + n0 + __popc(m1 & lanemask_lt)] = push[1];
+            sp += n0 + n1;
+            __syncwarp();
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) est += __shfl_xor_sync(kFull, est, off);
+    }
+    if (lane == 0) {
+        a.schedule[kSchedHeader + tile] = est;
+        const uint32_t key = est ? (uint32_t)__clz(est) : 32u;  // larger estimate -> smaller key
+        atomicAdd(&a.schedule[1 + key], 1u);
+    }
+}
+
+__global__ void sched_scan_kernel(uint32_t *sched) {
+    if (threadIdx.x != 0) return;
+    uint32_t acc = 0;
+    for (int k = 0; k <= 32; k++) {
+        const uint32_t c = sched[1 + k];
+        sched[1 + k] = acc;
+        acc += c;
+    }
+}
+
+__global__ void sched_scatter_kernel(uint32_t *sched, int ntiles) {
+    const int tile = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tile >= ntiles) return;
+    const uint32_t est = sched[kSchedHeader + tile];
+    const uint32_t key = est ? (uint32_t)__clz(est) : 32u;
+    const uint32_t pos = atomicAdd(&sched[1 + key], 1u);
+    if (pos < (uint32_t)ntiles) sched[kSchedHeader + ntiles + pos] = (uint32_t)tile;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1114,13 +1245,45 @@ cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_
     a.tile_h = 32 / a.tile_w;
     const int bw = a.tile_w * kBlockWarpsX, bh = a.tile_h * kBlockWarpsY;
     dim3 grid((p.render_width + bw - 1) / bw, (p.render_height + bh - 1) / bh);
+    a.tiles_x = (int)grid.x;
+    a.ntiles = (int)(grid.x * grid.y);
+    a.schedule = nullptr;
+    const void *kern;
+    const bool sched = p.hitlist.schedule && a.ntiles > 0 &&
+                       (size_t)a.ntiles <= (gray_schedule_words_for(p.image_width, p.image_height) - kSchedHeader) / 2;
     switch (v & 3) {
-        case 0: trace_forward_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(a); break;
-        case 1: trace_forward_kernel<32, 4><<<grid, kFwdThreads, 0, s>>>(a); break;
-        case 2: trace_forward_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(a); break;
-        default: trace_forward_kernel<16, 6><<<grid, kFwdThreads, 0, s>>>(a); break;
+        case 0: kern = sched ? reinterpret_cast<const void *>(&trace_forward_sched_kernel<32, 1>)
+                             : reinterpret_cast<const void *>(&trace_forward_kernel<32, 1>); break;
+        case 1: kern = sched ? reinterpret_cast<const void *>(&trace_forward_sched_kernel<32, 4>)
+                             : reinterpret_cast<const void *>(&trace_forward_kernel<32, 4>); break;
+        case 2: kern = sched ? reinterpret_cast<const void *>(&trace_forward_sched_kernel<16, 1>)
+                             : reinterpret_cast<const void *>(&trace_forward_kernel<16, 1>); break;
+        default: kern = sched ? reinterpret_cast<const void *>(&trace_forward_sched_kernel<16, 6>)
+                              : reinterpret_cast<const void *>(&trace_forward_kernel<16, 6>); break;
     }
+    cudaError_t e;
+    if (sched) {
+        // densest tiles first: estimate, bucket, then a persistent grid that takes tiles in order
+        a.schedule = p.hitlist.schedule;
+        if ((e = cudaMemsetAsync(a.schedule, 0, sizeof(uint32_t) * kSchedHeader, s)) != cudaSuccess) return e;
+        tile_cost_kernel<<<a.ntiles, 32, 0, s>>>(a, bw, bh);
+        sched_scan_kernel<<<1, 32, 0, s>>>(a.schedule);
+        sched_scatter_kernel<<<(a.ntiles + 255) / 256, 256, 0, s>>>(a.schedule, a.ntiles);
+        int dev = 0, sms = 0, per_sm = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFwdThreads, 0)) != cudaSuccess)
+            return e;
+        const unsigned int want = (unsigned int)(sms * (per_sm > 0 ? per_sm : 1));
+        grid = dim3(want < (unsigned int)a.ntiles ? want : (unsigned int)a.ntiles, 1, 1);
+    }
+    void *args[] = {&a};
+    if ((e = cudaLaunchKernel(kern, grid, dim3(kFwdThreads), args, 0, s)) != cudaSuccess) return e;
     return cudaGetLastError();
+}
+
+size_t gray_schedule_words_for(uint32_t width, uint32_t height) {
+    return (size_t)kSchedHeader + 2 * (size_t)((width + 7) / 8) * (size_t)((height + 7) / 8);
 }
 
 cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int nviews,

@@ -124,6 +124,8 @@ typedef struct gray_hitlist {
     uint32_t *total_words;    /* [1] bump counter */
     uint32_t *pool;           /* [size] */
     uint32_t size;
+    uint32_t *schedule;       /* [gray_schedule_words(W_alloc, H_alloc)] work order of the forward's
+                                 pixel tiles (dense tiles first); NULL: tiles in launch order */
 } gray_hitlist;
 
 /* Scene-side workspace owned by the caller (sizes from gray_scene_workspace_sizes). */
@@ -210,6 +212,10 @@ int gray_render_batch(const gray_batch_scene *scenes, const gray_batch_view *vie
 
 /* Workspace sizes in 32-bit words for n Gaussians: sort_tmp_words. */
 size_t gray_sort_tmp_words(int32_t n);
+
+/* Words of gray_hitlist.schedule for a width x height framebuffer (no counterpart in the reference:
+ * the forward estimates each pixel tile's work from the BVH and runs the densest tiles first). */
+size_t gray_schedule_words(uint32_t width, uint32_t height);
 
 /* Raytracer::forward_pass (cuda/raytracer.h:88-102): counts the call, resets the backward
  * hit list and was_visible, evaluates SH colours (if enable_sh) and traces the render

@@ -532,8 +532,10 @@ void orc_lbvh_build(int n, const float *aabb, const uint8_t *visible, orc_bvh *o
             out->int_parent[gamma + 1] = i;
         }
         float *nd = out->nodes + 16 * (size_t)i;
+        uint32_t leaves = (uint32_t)(hi_i - lo_i + 1); /* word 14: leaves below the node */
         memcpy(nd + 12, &c0, 4);
         memcpy(nd + 13, &c1, 4);
+        memcpy(nd + 14, &leaves, 4);
     }
     orc_lbvh_refit(out, aabb);
 }
