@@ -1126,6 +1126,10 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
     __shared__ uint32_t sstk[kWarps][kWideStack];
     __shared__ uint32_t scand[kWarps][kQueue];
     __shared__ CandCache scc[kWarps];
+    // the packet's scene and view parameters live in shared memory (read where used), which keeps
+    // them out of the registers the traversal needs
+    __shared__ TraceScene s_sc[kWarps];
+    __shared__ TraceKnobs s_k[kWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tile_h = 32 / tile_w;
     for (;;) {
@@ -1143,16 +1147,21 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
         const int px = (int)((local % tiles_x) * tile_w) + lane % tile_w;
         const int py = (int)((local / tiles_x) * tile_h) + lane / tile_w;
         const bool inside = px < (int)vw.width && py < (int)vw.height;
-        TraceKnobs k;
-        k.znear = vw.znear;
-        k.zfar = vw.zfar;
-        k.athr = bs.alpha_threshold;
-        k.pw = bs.exp_power;
-        k.tthr = bs.t_threshold;
-        k.render_depth = false;
-        const TraceScene sc{reinterpret_cast<const float4 *>(bs.geom), reinterpret_cast<const float4 *>(bs.l2w),
-                            reinterpret_cast<const float2 *>(bs.live),
-                            vw.channels, reinterpret_cast<const float4 *>(bs.nodes), bs.root_box, bs.n};
+        if (lane == 0) {
+            TraceKnobs &k = s_k[warp];
+            k.znear = vw.znear;
+            k.zfar = vw.zfar;
+            k.athr = bs.alpha_threshold;
+            k.pw = bs.exp_power;
+            k.tthr = bs.t_threshold;
+            k.render_depth = false;
+            s_sc[warp] = TraceScene{reinterpret_cast<const float4 *>(bs.geom), reinterpret_cast<const float4 *>(bs.l2w),
+                                    reinterpret_cast<const float2 *>(bs.live), vw.channels,
+                                    reinterpret_cast<const float4 *>(bs.nodes), bs.root_box, bs.n};
+        }
+        __syncwarp();
+        const TraceScene &sc = s_sc[warp];
+        const TraceKnobs &k = s_k[warp];
         const HitSink hs{nullptr, nullptr, 0};
         f3 ro = mk3(vw.origin[0], vw.origin[1], vw.origin[2]);
         f3 rd = mk3(0.0f, 0.0f, 0.0f);
