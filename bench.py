@@ -88,7 +88,9 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.proc = None
         self.gpu = gpu_index
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        import tempfile
+
+        self.path = os.path.join(tempfile.gettempdir(), f"gray_bench_clocks_{os.getpid()}.csv")
         self.t0 = self.t1 = None
 
     def start(self):

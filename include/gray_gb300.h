@@ -128,7 +128,7 @@ typedef struct gray_hitlist {
                                  pixel tiles (dense tiles first); NULL: tiles in launch order */
 } gray_hitlist;
 
-/* Scene-side workspace owned by the caller (sizes from gray_scene_workspace_sizes). */
+/* Scene-side workspace owned by the caller (sizes in the comments; sort_tmp from gray_sort_tmp_words). */
 typedef struct gray_scene {
     float *geom;        /* [N,12] snapshot rows (M | mu), M = diag(1/s) R^T          */
     float *l2w;         /* [N,12] snapshot rows (L | mu), L = R diag(s)               */

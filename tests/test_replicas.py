@@ -1,5 +1,5 @@
-"""Multi-GPU form of bench.py (replicas, SURVEY's row e: rays are independent given a replicated
-scene, no data-path collective) on the CPU with world_size-2 gloo ranks: each rank times its own
+"""Multi-GPU form of bench.py (replicas: rays are independent given a replicated scene, so there is
+no data-path collective) on the CPU with world_size-2 gloo ranks: each rank times its own
 replica, the job time is the max over ranks, the whole-job rate counts every rank's units, ranks
 render different views, and the reference arm runs on rank 0 only."""
 import os
