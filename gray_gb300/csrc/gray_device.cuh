@@ -21,10 +21,7 @@ namespace gray {
 // and the degree-7 Taylor polynomial of e^r in Horner form; 2^k applied through the exponent
 // field (two steps for results in the subnormal range).
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ float gexp(float x) {
-    if (x != x) return x;
-    if (x > 89.0f) return __int_as_float(0x7f800000);
-    if (x < -104.0f) return 0.0f;
+__device__ __forceinline__ float exp_poly(float x, int &ki) {
     float k = rintf(x * 0x1.715476p+0f);
     float r = fmaf(-k, 0x1.62ep-1f, x);
     r = fmaf(-k, 0x1.0bfbe8p-15f, r);
@@ -36,7 +33,21 @@ __device__ __forceinline__ float gexp(float x) {
     p = fmaf(p, r, 0x1.0p-1f);
     p = fmaf(p, r, 1.0f);
     p = fmaf(p, r, 1.0f);
-    int ki = (int)k;
+    ki = (int)k;
+    return p;
+}
+
+__device__ __forceinline__ float gexp(float x) {
+    int ki;
+    // |x| <= 87: k in [-126, 126], 2^k a normal float (the hit loop's case: one test)
+    if (fabsf(x) <= 87.0f) {
+        float p = exp_poly(x, ki);
+        return p * __int_as_float((ki + 127) << 23);
+    }
+    if (x != x) return x;
+    if (x > 89.0f) return __int_as_float(0x7f800000);
+    if (x < -104.0f) return 0.0f;
+    float p = exp_poly(x, ki);
     if (ki > 127) {
         p = p * 2.0f;
         ki -= 1;
@@ -49,20 +60,7 @@ __device__ __forceinline__ float gexp(float x) {
 }
 
 // log: x = m 2^e, m in [sqrt(1/2), sqrt(2)]; log m = 2 atanh(s), s = (m-1)/(m+1), series to s^11.
-__device__ __forceinline__ float glog(float x) {
-    if (x != x) return x;
-    if (x < 0.0f) return __int_as_float(0x7fc00000);
-    if (x == 0.0f) return __int_as_float(0xff800000);
-    if (x == __int_as_float(0x7f800000)) return x;
-    uint32_t u = __float_as_uint(x);
-    int e = 0;
-    if (u < 0x00800000u) {
-        x = x * 0x1.0p23f;
-        u = __float_as_uint(x);
-        e = -23;
-    }
-    e += (int)(u >> 23) - 127;
-    float m = __uint_as_float((u & 0x007fffffu) | 0x3f800000u);
+__device__ __forceinline__ float log_poly(float m, int e) {
     if (m > 0x1.6a09e6p+0f) {
         m = m * 0.5f;
         e += 1;
@@ -79,6 +77,20 @@ __device__ __forceinline__ float glog(float x) {
     float lm = fmaf(two_s * z, q, two_s);
     float ef = (float)e;
     return fmaf(ef, 0x1.62ep-1f, fmaf(ef, 0x1.0bfbe8p-15f, lm));
+}
+
+__device__ __forceinline__ float glog(float x) {
+    uint32_t u = __float_as_uint(x);
+    // positive normal x (the hit loop's case: one test)
+    if (u - 0x00800000u < 0x7f000000u)
+        return log_poly(__uint_as_float((u & 0x007fffffu) | 0x3f800000u), (int)(u >> 23) - 127);
+    if (x != x) return x;
+    if (x < 0.0f) return __int_as_float(0x7fc00000);
+    if (x == 0.0f) return __int_as_float(0xff800000);
+    if (x == __int_as_float(0x7f800000)) return x;
+    x = x * 0x1.0p23f;  // positive subnormal
+    u = __float_as_uint(x);
+    return log_poly(__uint_as_float((u & 0x007fffffu) | 0x3f800000u), (int)(u >> 23) - 127 - 23);
 }
 
 __device__ __forceinline__ float gpow(float a, float b) { return gexp(b * glog(a)); }
