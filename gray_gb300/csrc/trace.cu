@@ -386,8 +386,9 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
                 if (lane < take) node = stk[sp - 1 - lane];
                 __syncwarp();
                 sp -= take;
-                bool p0 = false, p1 = false;
-                uint32_t c0 = 0, c1 = 0;
+                // children as (a, b) = (nearer, farther) along the packet's mean direction
+                bool pa = false, pb = false;
+                uint32_t ca = 0, cb = 0;
                 if (node != GRAY_NULL) {
                     if (node >= (uint32_t)(n - 1)) {
                         raise_status(status, GRAY_STATUS_STACK_OVERFLOW);
@@ -396,30 +397,40 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
                                      q2 = sc.nodes[4 * node + 2], q3 = sc.nodes[4 * node + 3];
                         const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
                         const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
-                        c0 = __float_as_uint(q3.x);
-                        c1 = __float_as_uint(q3.y);
-                        p0 = frustum_box(fr, b0min, b0max);
-                        p1 = frustum_box(fr, b1min, b1max);
+                        const uint32_t c0 = __float_as_uint(q3.x), c1 = __float_as_uint(q3.y);
+                        const bool p0 = frustum_box(fr, b0min, b0max), p1 = frustum_box(fr, b1min, b1max);
+                        // box centres (times 2) projected on the mean direction; the origin is common
+                        const float s0 = fmaf(q0.z + q1.y, fr.n[4][2], fmaf(q0.y + q1.x, fr.n[4][1], (q0.x + q0.w) * fr.n[4][0]));
+                        const float s1 = fmaf(q2.x + q2.w, fr.n[4][2], fmaf(q1.w + q2.z, fr.n[4][1], (q1.z + q2.y) * fr.n[4][0]));
+                        const bool sw = s1 < s0;
+                        ca = sw ? c1 : c0;
+                        cb = sw ? c0 : c1;
+                        pa = sw ? p1 : p0;
+                        pb = sw ? p0 : p1;
                     }
                 }
-                const bool i0 = p0 && !(c0 & GRAY_LEAF_BIT), i1 = p1 && !(c1 & GRAY_LEAF_BIT);
-                const bool l0 = p0 && (c0 & GRAY_LEAF_BIT) && (c0 & ~GRAY_LEAF_BIT) < (uint32_t)n;
-                const bool l1 = p1 && (c1 & GRAY_LEAF_BIT) && (c1 & ~GRAY_LEAF_BIT) < (uint32_t)n;
-                const uint32_t m0 = __ballot_sync(kFull, i0), m1 = __ballot_sync(kFull, i1);
-                const int n0 = __popc(m0), n1 = __popc(m1);
-                if (sp + n0 + n1 > kWideStack) {
+                const bool ia = pa && !(ca & GRAY_LEAF_BIT), ib = pb && !(cb & GRAY_LEAF_BIT);
+                const bool la = pa && (ca & GRAY_LEAF_BIT) && (ca & ~GRAY_LEAF_BIT) < (uint32_t)n;
+                const bool lb = pb && (cb & GRAY_LEAF_BIT) && (cb & ~GRAY_LEAF_BIT) < (uint32_t)n;
+                // The popped nodes are in visit order (lane 0 took the top).  Their internal children
+                // go back so that the next pops see lane 0's nearer child first, then its farther
+                // one, then lane 1's, ...; the leaves are queued in the same order.
+                const uint32_t ma = __ballot_sync(kFull, ia), mb = __ballot_sync(kFull, ib);
+                const int ni = __popc(ma) + __popc(mb);
+                if (sp + ni > kWideStack) {
                     ok = false;  // frontier too wide for the shared stack
                     break;
                 }
-                if (i0) stk[sp + __popc(m0 & lanemask_lt)] = c0;
-                if (i1) stk[sp + n0 + __popc(m1 & lanemask_lt)] = c1;
-                sp += n0 + n1;
+                const int above = __popc(ma & lanemask_lt) + __popc(mb & lanemask_lt);
+                if (ia) stk[sp + ni - 1 - above] = ca;
+                if (ib) stk[sp + ni - 1 - above - (ia ? 1 : 0)] = cb;
+                sp += ni;
                 // queue the leaves found (nc < kCand before the step, at most 64 added)
-                const uint32_t q0m = __ballot_sync(kFull, l0), q1m = __ballot_sync(kFull, l1);
-                const int lq0 = __popc(q0m);
-                if (l0) cand[nc + __popc(q0m & lanemask_lt)] = c0 & ~GRAY_LEAF_BIT;
-                if (l1) cand[nc + lq0 + __popc(q1m & lanemask_lt)] = c1 & ~GRAY_LEAF_BIT;
-                nc += lq0 + __popc(q1m);
+                const uint32_t qa = __ballot_sync(kFull, la), qb = __ballot_sync(kFull, lb);
+                const int before = nc + __popc(qa & lanemask_lt) + __popc(qb & lanemask_lt);
+                if (la) cand[before] = ca & ~GRAY_LEAF_BIT;
+                if (lb) cand[before + (la ? 1 : 0)] = cb & ~GRAY_LEAF_BIT;
+                nc += __popc(qa) + __popc(qb);
                 __syncwarp();
             }
         }
