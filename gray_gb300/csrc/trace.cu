@@ -216,71 +216,79 @@ __device__ __forceinline__ void stack_push(uint32_t &stk0, uint32_t &stk1, int &
     }
 }
 
-// Frustum of a packet of primary rays sharing one origin: four side planes through the origin and
+// Frustum of a packet of primary rays sharing one origin o: four side planes through the origin and
 // the plane through the origin orthogonal to the packet's mean direction (nothing behind it can be
-// hit).  Normals point inside.  Stored per warp in shared memory.
+// hit).  Normals n point inside.  Stored per warp in shared memory as per-plane constants of the
+// two tests below: pn[p] = (n, box threshold), pa[p] = (|n|, ellipsoid threshold).
 struct Frustum {
-    float o[3];
-    float n[5][3];
+    float4 pn[5];
+    float4 pa[5];
 };
 
 // Frustum of the rays through the pixels [x0, x1] x [y0, y1] of a pinhole camera: the rays of the
-// corner pixels span a convex cone that contains every ray of the rectangle.
-__device__ __forceinline__ void make_frustum(Frustum &fr, f3 o, const f3 d[4]) {
-    fr.o[0] = o.x;
-    fr.o[1] = o.y;
-    fr.o[2] = o.z;
+// corner pixels span a convex cone that contains every ray of the rectangle.  root_box bounds every
+// box and mean the tests will see, which bounds their rounding error: with M the largest finite
+// coordinate magnitude of the root box, the tests' sums have magnitude at most |n|_1 (4M + 2|o|_1)
+// and a few roundings of 2^-24 each; the thresholds leave 1e-5 of that (about 170 roundings).
+// Boxes with an infinite or NaN coordinate (beyond M) give an infinite or NaN sum and always pass.
+__device__ __forceinline__ void make_frustum(Frustum &fr, f3 o, const f3 d[4], const float *root_box) {
     const f3 c = mk3(d[0].x + d[1].x + d[2].x + d[3].x, d[0].y + d[1].y + d[2].y + d[3].y,
                      d[0].z + d[1].z + d[2].z + d[3].z);
+    float m = 0.0f;
 #pragma unroll
-    for (int e = 0; e < 4; e++) {
-        const f3 a = d[e], b = d[(e + 1) & 3];
-        f3 nn = mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-        if (dot3(nn, c) < 0.0f) nn = mk3(-nn.x, -nn.y, -nn.z);
-        fr.n[e][0] = nn.x;
-        fr.n[e][1] = nn.y;
-        fr.n[e][2] = nn.z;
+    for (int i = 0; i < 8; i++) {
+        const float v = fabsf(root_box[i]);
+        if (i != 3 && i != 7 && v <= 0x1.fffffep127f) m = fmaxf(m, v);
     }
-    fr.n[4][0] = c.x;
-    fr.n[4][1] = c.y;
-    fr.n[4][2] = c.z;
+    const float o1 = fabsf(o.x) + fabsf(o.y) + fabsf(o.z);
+#pragma unroll
+    for (int e = 0; e < 5; e++) {
+        f3 nn = c;
+        if (e < 4) {
+            const f3 a = d[e], b = d[(e + 1) & 3];
+            nn = mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+            if (dot3(nn, c) < 0.0f) nn = mk3(-nn.x, -nn.y, -nn.z);
+        }
+        const float n1 = fabsf(nn.x) + fabsf(nn.y) + fabsf(nn.z);
+        const float no = fdot3(nn, o);
+        const float mbox = 1e-5f * n1 * (4.0f * m + 2.0f * o1) + 1e-30f;
+        const float mell = 1e-5f * n1 * (3.0f * m + o1) + 1e-30f;
+        fr.pn[e] = make_float4(nn.x, nn.y, nn.z, 2.0f * no - mbox);
+        fr.pa[e] = make_float4(fabsf(nn.x), fabsf(nn.y), fabsf(nn.z), no - mell);
+    }
 }
 
 // Conservative box-frustum test: false only when the box lies entirely outside one plane by more
-// than a rounding margin.
+// than a rounding margin.  The box's largest signed distance along n, times two, is
+// n.(bmin + bmax) + |n|.(bmax - bmin) - 2 n.o.  A NaN never culls.
 __device__ __forceinline__ bool frustum_box(const Frustum &fr, const float bmin[3], const float bmax[3]) {
+    const float sx = bmin[0] + bmax[0], sy = bmin[1] + bmax[1], sz = bmin[2] + bmax[2];
+    const float dx = bmax[0] - bmin[0], dy = bmax[1] - bmin[1], dz = bmax[2] - bmin[2];
 #pragma unroll
     for (int p = 0; p < 5; p++) {
-        const float nx = fr.n[p][0], ny = fr.n[p][1], nz = fr.n[p][2];
-        const float vx = (nx >= 0.0f ? bmax[0] : bmin[0]) - fr.o[0];
-        const float vy = (ny >= 0.0f ? bmax[1] : bmin[1]) - fr.o[1];
-        const float vz = (nz >= 0.0f ? bmax[2] : bmin[2]) - fr.o[2];
-        const float sdist = fmaf(nz, vz, fmaf(ny, vy, nx * vx));
-        const float margin = 1e-5f * (fabsf(nx) + fabsf(ny) + fabsf(nz)) * (fabsf(vx) + fabsf(vy) + fabsf(vz)) + 1e-30f;
-        if (sdist < -margin) return false;
+        const float4 n = fr.pn[p], a = fr.pa[p];
+        const float v = fmaf(a.z, dz, fmaf(a.y, dy, fmaf(a.x, dx, fmaf(n.z, sz, fmaf(n.y, sy, n.x * sx)))));
+        if (v < n.w) return false;
     }
     return true;
 }
 
 // Conservative frustum test of a Gaussian's support ellipsoid {mu + L u : |u| <= 1} (L, mu = the
 // snapshot's l2w rows): false only when the ellipsoid lies outside one plane by more than a rounding
-// margin.  The ellipsoid's extent along a normal n is |L^T n|.  A ray can only hit a Gaussian whose
-// ellipsoid it crosses, so a leaf whose ellipsoid misses the packet's frustum holds no hit of the
-// packet even when its box passed.
+// margin.  The ellipsoid's extent along a normal n is |L^T n| (taken 3e-5 larger for its own
+// rounding).  A ray can only hit a Gaussian whose ellipsoid it crosses, so a leaf whose ellipsoid
+// misses the packet's frustum holds no hit of the packet even when its box passed.
 __device__ __forceinline__ bool frustum_ellipsoid(const Frustum &fr, const float4 *l2w) {
     const float4 r0 = l2w[0], r1 = l2w[1], r2 = l2w[2];
-    const float vx = r0.w - fr.o[0], vy = r1.w - fr.o[1], vz = r2.w - fr.o[2];
 #pragma unroll
     for (int p = 0; p < 5; p++) {
-        const float nx = fr.n[p][0], ny = fr.n[p][1], nz = fr.n[p][2];
-        const float sdist = fmaf(nz, vz, fmaf(ny, vy, nx * vx));
-        const float e0 = fmaf(r2.x, nz, fmaf(r1.x, ny, r0.x * nx));
-        const float e1 = fmaf(r2.y, nz, fmaf(r1.y, ny, r0.y * nx));
-        const float e2 = fmaf(r2.z, nz, fmaf(r1.z, ny, r0.z * nx));
+        const float4 n = fr.pn[p];
+        const float sd = fmaf(n.z, r2.w, fmaf(n.y, r1.w, n.x * r0.w));
+        const float e0 = fmaf(r2.x, n.z, fmaf(r1.x, n.y, r0.x * n.x));
+        const float e1 = fmaf(r2.y, n.z, fmaf(r1.y, n.y, r0.y * n.x));
+        const float e2 = fmaf(r2.z, n.z, fmaf(r1.z, n.y, r0.z * n.x));
         const float ext = sqrtf(fmaf(e2, e2, fmaf(e1, e1, e0 * e0)));
-        const float n1 = fabsf(nx) + fabsf(ny) + fabsf(nz);
-        const float margin = 1e-5f * (n1 * (fabsf(vx) + fabsf(vy) + fabsf(vz)) + 3.0f * ext) + 1e-30f;
-        if (sdist + ext < -margin) return false;
+        if (fmaf(ext, 1.00003f, sd) < fr.pa[p].w) return false;
     }
     return true;
 }
@@ -400,8 +408,9 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
                         const uint32_t c0 = __float_as_uint(q3.x), c1 = __float_as_uint(q3.y);
                         const bool p0 = frustum_box(fr, b0min, b0max), p1 = frustum_box(fr, b1min, b1max);
                         // box centres (times 2) projected on the mean direction; the origin is common
-                        const float s0 = fmaf(q0.z + q1.y, fr.n[4][2], fmaf(q0.y + q1.x, fr.n[4][1], (q0.x + q0.w) * fr.n[4][0]));
-                        const float s1 = fmaf(q2.x + q2.w, fr.n[4][2], fmaf(q1.w + q2.z, fr.n[4][1], (q1.z + q2.y) * fr.n[4][0]));
+                        const float4 c = fr.pn[4];
+                        const float s0 = fmaf(q0.z + q1.y, c.z, fmaf(q0.y + q1.x, c.y, (q0.x + q0.w) * c.x));
+                        const float s1 = fmaf(q2.x + q2.w, c.z, fmaf(q1.w + q2.z, c.y, (q1.z + q2.y) * c.x));
                         const bool sw = s1 < s0;
                         ca = sw ? c1 : c0;
                         cb = sw ? c0 : c1;
@@ -782,7 +791,7 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
                              camera_ray(a.w2c, *a.fov, x1, y0, a.render_w, a.render_h, 0.0f, 0.0f),
                              camera_ray(a.w2c, *a.fov, x1, y1, a.render_w, a.render_h, 0.0f, 0.0f),
                              camera_ray(a.w2c, *a.fov, x0, y1, a.render_w, a.render_h, 0.0f, 0.0f)};
-            make_frustum(sfr[warp], o, d);
+            make_frustum(sfr[warp], o, d, a.root_box);
         }
         __syncwarp();
     }
@@ -881,7 +890,7 @@ __global__ void __launch_bounds__(32) tile_cost_kernel(const FwdArgs a, int bw, 
                              camera_ray(a.w2c, *a.fov, x1, y0, a.render_w, a.render_h, 0.0f, 0.0f),
                              camera_ray(a.w2c, *a.fov, x1, y1, a.render_w, a.render_h, 0.0f, 0.0f),
                              camera_ray(a.w2c, *a.fov, x0, y1, a.render_w, a.render_h, 0.0f, 0.0f)};
-            make_frustum(fr, o, d);
+            make_frustum(fr, o, d, a.root_box);
             stk[0] = 0u;
         }
         __syncwarp();
@@ -1184,7 +1193,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
                              camera_ray(vw.w2c, vw.fov_y, x1, y0, vw.width, vw.height, 0.0f, 0.0f),
                              camera_ray(vw.w2c, vw.fov_y, x1, y1, vw.width, vw.height, 0.0f, 0.0f),
                              camera_ray(vw.w2c, vw.fov_y, x0, y1, vw.width, vw.height, 0.0f, 0.0f)};
-            make_frustum(sfr[warp], ro, d);
+            make_frustum(sfr[warp], ro, d, s_sc[warp].root_box);
         }
         __syncwarp();
         RayResult r;
