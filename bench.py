@@ -53,6 +53,7 @@ def parse_args(argv):
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and served measurements")
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--no-served", action="store_true", help="skip the served measurement only")
+    ap.add_argument("--trace-variant", type=int, default=0, help="forward-kernel variant (0 = library default)")
     return ap.parse_args(argv)
 
 
@@ -212,6 +213,8 @@ def gpu_arm(a, rank, world, local_rank):
         g.sh_coeffs_rest.copy_(torch.from_numpy(sc.sh_rest))
         g.current_sh_degree.fill_(3)
     rt.cuda_module.rebuild_bvh()
+    if a.trace_variant:
+        rt.cuda_module.set_trace_variant(a.trace_variant)
     gen = torch.Generator().manual_seed(1234 + rank)
     target_host = torch.rand(3, a.height, a.width, generator=gen).pin_memory()
     target_dev = target_host.to(dev)

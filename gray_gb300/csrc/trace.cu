@@ -33,6 +33,14 @@ constexpr int kWideStack = 256;  // per-warp shared stack of the frustum travers
 constexpr int kCand = 32;        // leaves processed per flush (one per lane)
 constexpr int kQueue = 3 * kCand; // per-warp queue of leaves: < kCand before a step, + up to 64 per step
 constexpr int kSchedHeader = 64;  // schedule words before the per-tile estimates
+// Per pixel tile, the BVH frontier its frustum reaches (words: count, then up to kFrontierMax node or
+// leaf entries); a count of kFrontierNone means "start at the root".  A frontier goes onto the
+// traversal stack, so it leaves room there for the traversal's own pushes (up to 64 per step; the
+// stack above a frontier peaks near 70 entries on the benchmark scene).
+constexpr int kFrontierStride = 256;
+constexpr int kFrontierMax = 160;
+constexpr uint32_t kFrontierNone = 0xFFFFFFFFu;
+constexpr int kFrontierCutDefault = 64;  // frontier nodes hold at most this many leaves
 
 struct FwdArgs {
     uint32_t alloc_w, render_w, render_h;
@@ -46,6 +54,8 @@ struct FwdArgs {
     int display;  // forward_pass_display: colour only, whatever grads_enabled holds
     uint32_t *schedule;  // work order of the pixel tiles (null: tiles in launch order)
     int tiles_x, ntiles;
+    uint32_t *frontier;  // per-tile BVH frontiers (null: packets start at the root)
+    uint32_t frontier_cut;
     const uint32_t *total_num_calls;
     const float4 *geom, *l2w;
     const float2 *live;
@@ -359,13 +369,16 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
 // One full traversal of the packet (camera rays with a common origin) with the node work spread
 // over the lanes: each step pops up to 32 nodes, one per lane, tests their child boxes against the
 // packet frustum, pushes surviving internal children and queues surviving leaves; queued leaves
-// are then intersected by every lane with its own ray (on_leaf).  Returns false if the shared
-// stack overflowed (the caller then repeats the traversal per ray).
+// are then intersected by every lane with its own ray (on_leaf).  With a tile frontier (front[0,
+// *nfront), *nfront >= 0) the traversal starts there instead of at the root: the frontier goes onto
+// the stack with its first entry on top, and a frontier leaf is queued when it is popped.  Returns
+// false if the shared stack overflowed (the caller then repeats the traversal per ray).
 template <int KB>
 __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool want,
                                                  bool first, LaneState &st, unsigned long long (*kbuf)[kFwdThreads],
                                                  const Frustum &fr, uint32_t *stk, uint32_t *cand,
-                                                 CandCache &cc, int32_t *status) {
+                                                 CandCache &cc, const uint32_t *front, const int *nfront,
+                                                 int32_t *status) {
     const int lane = threadIdx.x & 31;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     const int n = sc.n;
@@ -376,9 +389,14 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
         on_leaf<KB>(sc, 0u, want, first, ro, rd, k, st, kbuf);
         return true;
     }
-    if (lane == 0) stk[0] = 0u;
+    int sp = nfront ? *nfront : -1, nc = 0;
+    if (sp >= 0 && sp <= kFrontierMax) {
+        for (int i = lane; i < sp; i += 32) stk[sp - 1 - i] = front[i];
+    } else {
+        if (lane == 0) stk[0] = 0u;
+        sp = 1;
+    }
     __syncwarp();
-    int sp = 1, nc = 0;
     bool ok = true, draining = false;
     long long budget = (long long)n;  // a valid tree pushes each internal node at most once per traversal
     for (;;) {
@@ -398,7 +416,10 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
                 bool pa = false, pb = false;
                 uint32_t ca = 0, cb = 0;
                 if (node != GRAY_NULL) {
-                    if (node >= (uint32_t)(n - 1)) {
+                    if (node & GRAY_LEAF_BIT) {
+                        ca = node;  // a leaf of the tile's frontier: queued below
+                        pa = true;
+                    } else if (node >= (uint32_t)(n - 1)) {
                         raise_status(status, GRAY_STATUS_STACK_OVERFLOW);
                     } else {
                         const float4 q0 = sc.nodes[4 * node], q1 = sc.nodes[4 * node + 1],
@@ -471,7 +492,8 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
                                           bool grads, const HitSink &hs, int32_t *status,
                                           unsigned long long (*kbuf)[kFwdThreads], RayResult &res,
                                           const Frustum *fr = nullptr, uint32_t *wstk = nullptr,
-                                          uint32_t *wcand = nullptr, CandCache *wcc = nullptr) {
+                                          uint32_t *wcand = nullptr, CandCache *wcc = nullptr,
+                                          const uint32_t *front = nullptr, const int *nfront = nullptr) {
     const int lane = threadIdx.x & 31;
     LaneState &st = res.st;
     st.lfx = 0;
@@ -497,7 +519,8 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
         st.ncand = 0;
         // ---------------- traversal ----------------
         bool per_ray = fr == nullptr;
-        if (!per_ray && !traverse_frustum<KB>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, *wcc, status)) {
+        if (!per_ray &&
+            !traverse_frustum<KB>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, *wcc, front, nfront, status)) {
             // the frustum traversal gave up (stack overflow): discard what it gathered, trace per ray
             st.kcount = 0;
             st.ncand = 0;
@@ -736,6 +759,8 @@ struct FwdShared {
     uint32_t sstk[kWarps][kWideStack];
     uint32_t scand[kWarps][kQueue];
     CandCache scc[kWarps];
+    uint32_t front[kFrontierMax];  // the tile's BVH frontier (frontier launches)
+    int nfront;                    // its length, or -1: traversals start at the root
 };
 
 // One block's pixel tile (bx, by): 2x2 packets of tile_w x tile_h pixels, one per warp.
@@ -782,6 +807,16 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
 
     // camera rays of the packet share the origin: trace with the frustum traversal
     const bool frustum = !*a.rays_from_python && !*a.jitter;
+    // the tile's frontier, read once by the block (every thread of the block gets here together)
+    {
+        const uint32_t *src = a.frontier ? a.frontier + (size_t)(by * a.tiles_x + bx) * kFrontierStride : nullptr;
+        const uint32_t cnt = src && frustum ? src[0] : kFrontierNone;
+        const bool use = cnt <= (uint32_t)kFrontierMax;
+        if (use)
+            for (uint32_t i = threadIdx.x; i < cnt; i += kFwdThreads) sh.front[i] = src[1 + i];
+        if (threadIdx.x == 0) sh.nfront = use ? (int)cnt : -1;
+        __syncthreads();
+    }
     if (frustum) {
         const int x0 = px - lane % a.tile_w, y0 = py - lane / a.tile_w;
         const int x1 = x0 + a.tile_w - 1, y1 = y0 + a.tile_h - 1;
@@ -797,7 +832,7 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
     }
     RayResult r;
     trace_ray<KB>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sh.sstk[warp],
-                  sh.scand[warp], &sh.scc[warp]);
+                  sh.scand[warp], &sh.scc[warp], sh.front, &sh.nfront);
 
     if (!inside) return;
     if (!alive) {
@@ -853,7 +888,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_sched_kernel(
     __shared__ uint32_t s_next;
     if (*a.render_ellipsoids) return;
     for (;;) {
-        __syncthreads();  // every thread is done with the previous tile (and s_next)
+        __syncthreads();  // every thread is done with the previous tile (s_next, the frontier)
         if (threadIdx.x == 0) s_next = atomicAdd(a.schedule, 1u);
         __syncthreads();
         const uint32_t t = s_next;
@@ -864,12 +899,17 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_sched_kernel(
 }
 
 // ---------------------------------------------------------------------------------------------
-// Work order of the forward's tiles.  A tile's work follows the number of Gaussians its rays meet
-// (per-packet time correlates 0.92 with hits), so the estimate is the number of leaves under the
-// BVH nodes its frustum reaches, cut where a node holds at most kCostCut leaves.  Tiles are then
-// counting-sorted by log2 of the estimate, largest first, so the launch does not end with a dense
-// tile started late.  Schedule words: [0] work counter, [1..33] bucket counts/cursors,
-// [kSchedHeader, +ntiles) estimates, [kSchedHeader + ntiles, +ntiles) order.
+// Work order of the forward's tiles and their BVH frontiers.  A tile's work follows the number of
+// Gaussians its rays meet (per-packet time correlates 0.92 with hits), so the estimate is the number
+// of leaves under the BVH nodes its frustum reaches, cut where a node holds at most `cut` leaves.
+// Tiles are then counting-sorted by log2 of the estimate, largest first, so the launch does not end
+// with a dense tile started late.  The nodes at the cut (and leaves reached above it) are the tile's
+// frontier: every ray of the tile that hits a Gaussian reaches it through one of them, so the tile's
+// packets start their traversals there instead of at the root (the top levels are walked once per
+// tile, not once per packet traversal).  The frontier is sorted by its boxes' centres along the
+// tile's mean direction, so packets visit it roughly front to back.  Schedule words: [0] work
+// counter, [1..33] bucket counts/cursors, [kSchedHeader, +ntiles) estimates, [kSchedHeader + ntiles,
+// +ntiles) order, then (when frontiers are on) kFrontierStride words per tile.
 // ---------------------------------------------------------------------------------------------
 constexpr int kCostCut = 512;
 constexpr int kCostStack = 256;
@@ -877,10 +917,15 @@ constexpr int kCostStack = 256;
 __global__ void __launch_bounds__(32) tile_cost_kernel(const FwdArgs a, int bw, int bh) {
     __shared__ Frustum fr;
     __shared__ uint32_t stk[kCostStack];
+    __shared__ float fkey[kFrontierStride];
+    __shared__ uint32_t fval[kFrontierStride];
     const int tile = blockIdx.x, lane = threadIdx.x;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     uint32_t est = 0;
     const int n = a.n;
+    const uint32_t cut = a.frontier_cut > 0 ? a.frontier_cut : (uint32_t)kCostCut;
+    bool complete = false;  // the walk reached every frontier entry and they fit
+    int nf = 0;
     if (!*a.rays_from_python && !*a.jitter && !*a.render_ellipsoids && n > 1) {
         const int x0 = (tile % a.tiles_x) * bw, y0 = (tile / a.tiles_x) * bh;
         const int x1 = min(x0 + bw, (int)a.render_w) - 1, y1 = min(y0 + bh, (int)a.render_h) - 1;
@@ -895,42 +940,137 @@ __global__ void __launch_bounds__(32) tile_cost_kernel(const FwdArgs a, int bw, 
         }
         __syncwarp();
         int sp = 1;
-        for (int guard = 0; sp > 0 && guard < 4096; guard++) {
+        complete = true;
+        for (int guard = 0; sp > 0; guard++) {
+            if (guard >= 4096) {
+                complete = false;
+                break;
+            }
             const int take = sp < 32 ? sp : 32;
             uint32_t node = GRAY_NULL;
             if (lane < take) node = stk[sp - 1 - lane];
             __syncwarp();
             sp -= take;
-            uint32_t push[2] = {GRAY_NULL, GRAY_NULL};
-            if (node != GRAY_NULL && node < (uint32_t)(n - 1)) {
-                const float4 q0 = a.nodes[4 * node], q1 = a.nodes[4 * node + 1], q2 = a.nodes[4 * node + 2],
-                             q3 = a.nodes[4 * node + 3];
-                const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
-                const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
-                const uint32_t c[2] = {__float_as_uint(q3.x), __float_as_uint(q3.y)};
-                const bool in[2] = {frustum_box(fr, b0min, b0max), frustum_box(fr, b1min, b1max)};
-#pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    if (!in[q]) continue;
-                    if (c[q] & GRAY_LEAF_BIT) {
-                        est += 1u;
-                    } else if (c[q] < (uint32_t)(n - 1)) {
-                        const uint32_t leaves = __float_as_uint(a.nodes[4 * c[q] + 3].z);
-                        if (leaves <= (uint32_t)kCostCut) est += leaves;
-                        else push[q] = c[q];
-                    }
+            // children as (a, b) = (nearer, farther) along the tile's mean direction, as the forward
+            uint32_t ca = 0, cb = 0;
+            bool pa = false, pb = false, bad = false;
+            float sa = 0.0f, sb = 0.0f;
+            if (node != GRAY_NULL) {
+                if (node >= (uint32_t)(n - 1)) {
+                    bad = true;
+                } else {
+                    const float4 q0 = a.nodes[4 * node], q1 = a.nodes[4 * node + 1], q2 = a.nodes[4 * node + 2],
+                                 q3 = a.nodes[4 * node + 3];
+                    const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
+                    const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
+                    const uint32_t c0 = __float_as_uint(q3.x), c1 = __float_as_uint(q3.y);
+                    const bool p0 = frustum_box(fr, b0min, b0max), p1 = frustum_box(fr, b1min, b1max);
+                    const float4 c = fr.pn[4];
+                    const float s0 = fmaf(q0.z + q1.y, c.z, fmaf(q0.y + q1.x, c.y, (q0.x + q0.w) * c.x));
+                    const float s1 = fmaf(q2.x + q2.w, c.z, fmaf(q1.w + q2.z, c.y, (q1.z + q2.y) * c.x));
+                    const bool sw = s1 < s0;
+                    ca = sw ? c1 : c0;
+                    cb = sw ? c0 : c1;
+                    pa = sw ? p1 : p0;
+                    pb = sw ? p0 : p1;
+                    sa = sw ? s1 : s0;
+                    sb = sw ? s0 : s1;
                 }
             }
-            const uint32_t m0 = __ballot_sync(kFull, push[0] != GRAY_NULL), m1 = __ballot_sync(kFull, push[1] != GRAY_NULL);
-            const int n0 = __popc(m0), n1 = __popc(m1);
-            if (sp + n0 + n1 > kCostStack) break;  // an estimate from what was reached is enough
-            if (push[0] != GRAY_NULL) stk[sp + __popc(m0 & lanemask_lt)] = push[0];
-            if (push[1] != GRAY_NULL) stk[sp + n0 + __popc(m1 & lanemask_lt)] = push[1];
-            sp += n0 + n1;
+            // internal children above the cut are walked further; leaves and nodes at the cut are
+            // frontier entries
+            bool ia = false, ib = false, fa = false, fb = false;
+            if (pa) {
+                if (ca & GRAY_LEAF_BIT) {
+                    fa = (ca & ~GRAY_LEAF_BIT) < (uint32_t)n;
+                    bad = bad || !fa;
+                    est += fa ? 1u : 0u;
+                } else if (ca < (uint32_t)(n - 1)) {
+                    const uint32_t leaves = __float_as_uint(a.nodes[4 * ca + 3].z);
+                    ia = leaves > cut;
+                    fa = !ia;
+                    if (fa) est += leaves;
+                } else {
+                    bad = true;
+                }
+            }
+            if (pb) {
+                if (cb & GRAY_LEAF_BIT) {
+                    fb = (cb & ~GRAY_LEAF_BIT) < (uint32_t)n;
+                    bad = bad || !fb;
+                    est += fb ? 1u : 0u;
+                } else if (cb < (uint32_t)(n - 1)) {
+                    const uint32_t leaves = __float_as_uint(a.nodes[4 * cb + 3].z);
+                    ib = leaves > cut;
+                    fb = !ib;
+                    if (fb) est += leaves;
+                } else {
+                    bad = true;
+                }
+            }
+            // a malformed tree: leave it to the forward's own checks (root start)
+            if (__any_sync(kFull, bad)) complete = false;
+            const uint32_t ma = __ballot_sync(kFull, ia), mb = __ballot_sync(kFull, ib);
+            const int ni = __popc(ma) + __popc(mb);
+            if (sp + ni > kCostStack) {
+                complete = false;  // an estimate from what was reached is enough
+                break;
+            }
+            const int above = __popc(ma & lanemask_lt) + __popc(mb & lanemask_lt);
+            if (ia) stk[sp + ni - 1 - above] = ca;
+            if (ib) stk[sp + ni - 1 - above - (ia ? 1 : 0)] = cb;
+            sp += ni;
+            const uint32_t qa = __ballot_sync(kFull, fa), qb = __ballot_sync(kFull, fb);
+            const int before = nf + __popc(qa & lanemask_lt) + __popc(qb & lanemask_lt);
+            if (fa && before < kFrontierStride - 1) {
+                fkey[before] = sa;
+                fval[before] = ca;
+            }
+            if (fb && before + (fa ? 1 : 0) < kFrontierStride - 1) {
+                fkey[before + (fa ? 1 : 0)] = sb;
+                fval[before + (fa ? 1 : 0)] = cb;
+            }
+            nf += __popc(qa) + __popc(qb);
             __syncwarp();
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) est += __shfl_xor_sync(kFull, est, off);
+    }
+    if (a.frontier) {
+        uint32_t *out = a.frontier + (size_t)tile * kFrontierStride;
+        if (complete && nf <= kFrontierMax) {
+            // bitonic sort of the entries by key (padding sorts last); NaN keys compare false
+            int p2 = 32;
+            while (p2 < nf) p2 <<= 1;
+            for (int i = nf + lane; i < p2; i += 32) {
+                fkey[i] = __int_as_float(0x7f800000);
+                fval[i] = GRAY_NULL;
+            }
+            __syncwarp();
+            for (int k = 2; k <= p2; k <<= 1) {
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    for (int i = lane; i < p2; i += 32) {
+                        const int ixj = i ^ j;
+                        if (ixj > i) {
+                            const float ki = fkey[i], kj = fkey[ixj];
+                            const bool up = (i & k) == 0;
+                            if (up ? (kj < ki) : (ki < kj)) {
+                                fkey[i] = kj;
+                                fkey[ixj] = ki;
+                                const uint32_t v = fval[i];
+                                fval[i] = fval[ixj];
+                                fval[ixj] = v;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+            for (int i = lane; i < nf; i += 32) out[1 + i] = fval[i];
+            if (lane == 0) out[0] = (uint32_t)nf;
+        } else if (lane == 0) {
+            out[0] = kFrontierNone;
+        }
     }
     if (lane == 0) {
         a.schedule[kSchedHeader + tile] = est;
@@ -1256,6 +1396,9 @@ static FwdArgs forward_args(const gray_params &p, bool display) {
     a.ellipsoid_min_opacity = p.config.ellipsoid_min_opacity;
     a.tile_w = 8;
     a.tile_h = 4;
+    a.schedule = nullptr;
+    a.frontier = nullptr;
+    a.frontier_cut = 0;
     return a;
 }
 
@@ -1268,8 +1411,10 @@ cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s
 
 cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_t s) {
     FwdArgs a = forward_args(p, display);
-    // variant: bits 0-1 select (buffer size, register cap), bit 2 the packet shape
+    // variant: bits 0-1 select (buffer size, register cap), bit 2 the packet shape, bits 3-4 the
+    // tile frontier's cut (64 leaves, 32, 128, no frontier)
     const int v = p.trace_variant > 0 ? p.trace_variant : kDefaultTraceVariant;
+    const int fcut = (v >> 3) & 3;
     a.tile_w = (v & 4) ? 4 : 8;
     a.tile_h = 32 / a.tile_w;
     const int bw = a.tile_w * kBlockWarpsX, bh = a.tile_h * kBlockWarpsY;
@@ -1278,8 +1423,8 @@ cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_
     a.ntiles = (int)(grid.x * grid.y);
     a.schedule = nullptr;
     const void *kern;
-    const bool sched = p.hitlist.schedule && a.ntiles > 0 &&
-                       (size_t)a.ntiles <= (gray_schedule_words_for(p.image_width, p.image_height) - kSchedHeader) / 2;
+    const size_t words = gray_schedule_words_for(p.image_width, p.image_height);
+    const bool sched = p.hitlist.schedule && a.ntiles > 0 && (size_t)a.ntiles <= (words - kSchedHeader) / 2;
     switch (v & 3) {
         case 0: kern = sched ? reinterpret_cast<const void *>(&trace_forward_sched_kernel<32, 1>)
                              : reinterpret_cast<const void *>(&trace_forward_kernel<32, 1>); break;
@@ -1294,6 +1439,9 @@ cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_
     if (sched) {
         // densest tiles first: estimate, bucket, then a persistent grid that takes tiles in order
         a.schedule = p.hitlist.schedule;
+        a.frontier_cut = fcut == 0 ? kFrontierCutDefault : fcut == 1 ? 32u : fcut == 2 ? 128u : 0u;
+        if (a.frontier_cut > 0 && (size_t)a.ntiles <= (words - kSchedHeader) / (2 + kFrontierStride))
+            a.frontier = a.schedule + kSchedHeader + 2 * (size_t)a.ntiles;
         if ((e = cudaMemsetAsync(a.schedule, 0, sizeof(uint32_t) * kSchedHeader, s)) != cudaSuccess) return e;
         tile_cost_kernel<<<a.ntiles, 32, 0, s>>>(a, bw, bh);
         sched_scan_kernel<<<1, 32, 0, s>>>(a.schedule);
@@ -1312,7 +1460,12 @@ cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_
 }
 
 size_t gray_schedule_words_for(uint32_t width, uint32_t height) {
-    return (size_t)kSchedHeader + 2 * (size_t)((width + 7) / 8) * (size_t)((height + 7) / 8);
+    // estimates and order for any tile shape (tiles of at least 8x8 pixels), frontiers for tiles
+    // of 8x16 or 16x8 pixels (the forward's block tiles)
+    const size_t t8 = (size_t)((width + 7) / 8) * (size_t)((height + 7) / 8);
+    const size_t ta = (size_t)((width + 7) / 8) * (size_t)((height + 15) / 16);
+    const size_t tb = (size_t)((width + 15) / 16) * (size_t)((height + 7) / 8);
+    return (size_t)kSchedHeader + 2 * t8 + (ta > tb ? ta : tb) * kFrontierStride;
 }
 
 cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int nviews,

@@ -125,7 +125,8 @@ typedef struct gray_hitlist {
     uint32_t *pool;           /* [size] */
     uint32_t size;
     uint32_t *schedule;       /* [gray_schedule_words(W_alloc, H_alloc)] work order of the forward's
-                                 pixel tiles (dense tiles first); NULL: tiles in launch order */
+                                 pixel tiles (dense tiles first) and each tile's BVH frontier;
+                                 NULL: tiles in launch order, traversals from the root */
 } gray_hitlist;
 
 /* Scene-side workspace owned by the caller (sizes in the comments; sort_tmp from gray_sort_tmp_words). */
@@ -163,8 +164,9 @@ typedef struct gray_params {
     gray_scene scene;
     int32_t *status; /* device int32, GRAY_STATUS_* bits */
     /* forward-trace kernel variant (0 = library default): bits 0-1 = physical hit buffer of
-     * 32 or 16 keys and register cap, bit 2 = 8x4 or 4x8 pixel packets.  Results are identical
-     * for every variant; only speed differs (see gray_gb300.autotune). */
+     * 32 or 16 keys and register cap, bit 2 = 8x4 or 4x8 pixel packets, bits 3-4 = where a pixel
+     * tile's traversals start (BVH nodes of at most 64, 32 or 128 leaves that the tile's frustum
+     * reaches, or the root).  Results are identical for every variant; only speed differs. */
     int32_t trace_variant;
 } gray_params;
 
@@ -214,7 +216,8 @@ int gray_render_batch(const gray_batch_scene *scenes, const gray_batch_view *vie
 size_t gray_sort_tmp_words(int32_t n);
 
 /* Words of gray_hitlist.schedule for a width x height framebuffer (no counterpart in the reference:
- * the forward estimates each pixel tile's work from the BVH and runs the densest tiles first). */
+ * the forward estimates each pixel tile's work from the BVH, runs the densest tiles first and starts
+ * each tile's traversals at the BVH nodes the tile's frustum reaches). */
 size_t gray_schedule_words(uint32_t width, uint32_t height);
 
 /* Raytracer::forward_pass (cuda/raytracer.h:88-102): counts the call, resets the backward
