@@ -34,7 +34,7 @@ class BatchViewC(ctypes.Structure):
     _fields_ = [("origin", ctypes.c_float * 3), ("w2c", ctypes.c_float * 9), ("fov_y", ctypes.c_float),
                 ("znear", ctypes.c_float), ("zfar", ctypes.c_float), ("width", ctypes.c_uint32),
                 ("height", ctypes.c_uint32), ("scene", ctypes.c_uint32), ("packet_offset", ctypes.c_uint32),
-                ("pad", ctypes.c_uint32), ("out_offset", ctypes.c_uint64), ("channels", ctypes.c_void_p)]
+                ("group_offset", ctypes.c_uint32), ("out_offset", ctypes.c_uint64), ("channels", ctypes.c_void_p)]
 
 
 def _bind():
@@ -42,13 +42,17 @@ def _bind():
     if not getattr(L, "_batch_bound", False):
         L.gray_batch_packets.restype = ctypes.c_uint32
         L.gray_batch_packets.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32]
+        L.gray_batch_groups.restype = ctypes.c_uint32
+        L.gray_batch_groups.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32]
+        L.gray_frontier_words.restype = ctypes.c_uint32
+        L.gray_frontier_words.argtypes = []
         L.gray_batch_prep.restype = ctypes.c_int
         L.gray_batch_prep.argtypes = [ctypes.POINTER(_lib.ParamsC), ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                                       ctypes.c_void_p]
         L.gray_render_batch.restype = ctypes.c_int
         L.gray_render_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32,
-                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
-                                        ctypes.c_void_p, ctypes.c_void_p]
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                        ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
         L._batch_bound = True
     return L
 
@@ -83,6 +87,8 @@ class _Plan:
     offsets: list
     total_packets: int
     counter: torch.Tensor
+    frontier: torch.Tensor         # per packet group: its BVH frontier (GRAY_FRONTIER_WORDS words)
+    total_groups: int
     graph: object = None
 
 
@@ -149,15 +155,18 @@ class BatchRenderer:
         out = torch.empty(max(total, 1), device=self.device)
         vh = torch.zeros(V * ctypes.sizeof(BatchViewC), dtype=torch.uint8).pin_memory()
         oh = torch.zeros(V, 3, dtype=torch.float32).pin_memory()
+        groups = sum(int(self.L.gray_batch_groups(c.image_width, c.image_height, variant)) for _, c in reqs)
+        frontier = torch.empty(max(groups, 1) * int(self.L.gray_frontier_words()), device=self.device,
+                               dtype=torch.int32)
         plan = _Plan(sig, variant, bps, vh, torch.zeros_like(vh, device=self.device), oh,
                      torch.zeros(V, 3, device=self.device), channels, view_rows, out, offsets, 0,
-                     torch.zeros(1, device=self.device, dtype=torch.int32))
+                     torch.zeros(1, device=self.device, dtype=torch.int32), frontier, groups)
         self._write_views(plan, reqs)
         return plan
 
     def _write_views(self, plan, reqs):
         arr = (BatchViewC * len(reqs)).from_buffer(plan.views_host.numpy())
-        packets = 0
+        packets = groups = 0
         for i, (s, cam) in enumerate(reqs):
             rot = cam.rotation_c2w_blender()
             w2c = rot.T.astype(np.float32)
@@ -172,6 +181,8 @@ class BatchRenderer:
             v.scene = s
             v.packet_offset = packets
             packets += int(self.L.gray_batch_packets(cam.image_width, cam.image_height, plan.variant))
+            v.group_offset = groups
+            groups += int(self.L.gray_batch_groups(cam.image_width, cam.image_height, plan.variant))
             v.out_offset = plan.offsets[i]
             sc, row = plan.view_rows[i]
             v.channels = plan.channels[sc][row].data_ptr()
@@ -197,7 +208,9 @@ class BatchRenderer:
         rc = self.L.gray_render_batch(ctypes.c_void_p(self._scenes_dev.data_ptr()),
                                       ctypes.c_void_p(plan.views_dev.data_ptr()), len(plan.view_rows),
                                       plan.total_packets, ctypes.c_void_p(plan.out.data_ptr()),
-                                      ctypes.c_void_p(plan.counter.data_ptr()), plan.variant, plan.blocks_per_sm,
+                                      ctypes.c_void_p(plan.counter.data_ptr()),
+                                      ctypes.c_void_p(plan.frontier.data_ptr()), plan.total_groups,
+                                      plan.variant, plan.blocks_per_sm,
                                       ctypes.c_void_p(self.status.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
         _check(self.L, rc, "gray_render_batch")
 

@@ -222,6 +222,15 @@ uint32_t gray_batch_packets(uint32_t width, uint32_t height, int32_t variant) {
     return ((width + tw - 1) / tw) * ((height + th - 1) / th);
 }
 
+uint32_t gray_batch_groups(uint32_t width, uint32_t height, int32_t variant) {
+    const int v = variant > 0 ? variant : gray::kDefaultTraceVariant;
+    const uint32_t tw = (v & 4) ? 4u : 8u, th = 32u / tw;
+    const uint32_t tx = (width + tw - 1) / tw, ty = (height + th - 1) / th;
+    return ((tx + 1) / 2) * ((ty + 1) / 2);
+}
+
+uint32_t gray_frontier_words(void) { return GRAY_FRONTIER_WORDS; }
+
 int gray_batch_prep(const gray_params *p, const float *origins, int32_t nviews, float *channels_out, void *stream) {
     int e = check_common(p);
     if (e) return e;
@@ -233,14 +242,15 @@ int gray_batch_prep(const gray_params *p, const float *origins, int32_t nviews, 
 }
 
 int gray_render_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int32_t nviews,
-                      uint32_t total_packets, float *out, uint32_t *work_counter, int32_t variant,
-                      int32_t blocks_per_sm, int32_t *status, void *stream) {
+                      uint32_t total_packets, float *out, uint32_t *work_counter, uint32_t *frontier,
+                      uint32_t total_groups, int32_t variant, int32_t blocks_per_sm, int32_t *status,
+                      void *stream) {
     if (nviews <= 0 || !scenes || !views || !out || !work_counter)
         return fail(GRAY_ERR_INVALID_ARGUMENT, "render_batch: missing buffers");
     if (blocks_per_sm < 0 || blocks_per_sm > 32) return fail(GRAY_ERR_OUT_OF_RANGE, "render_batch: blocks_per_sm");
     cudaStream_t s = (cudaStream_t)stream;
     GRAY_LAUNCH("trace_batch", gray::launch_trace_batch(scenes, views, nviews, total_packets, out, work_counter,
-                                                        variant, blocks_per_sm, status, s));
+                                                        frontier, total_groups, variant, blocks_per_sm, status, s));
     return GRAY_OK;
 }
 

@@ -33,8 +33,9 @@ size_t gray_schedule_words_for(uint32_t width, uint32_t height);
 cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s);
 cudaError_t launch_trace_backward(const gray_params &p, cudaStream_t s);
 cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int nviews,
-                               uint32_t total_packets, float *out, uint32_t *counter, int variant, int blocks_per_sm,
-                               int32_t *status, cudaStream_t s);
+                               uint32_t total_packets, float *out, uint32_t *counter, uint32_t *frontier,
+                               uint32_t total_groups, int variant, int blocks_per_sm, int32_t *status,
+                               cudaStream_t s);
 
 // adam.cu
 cudaError_t launch_adam(const gray_params &p, cudaStream_t s);

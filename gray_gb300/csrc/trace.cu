@@ -33,12 +33,13 @@ constexpr int kWideStack = 256;  // per-warp shared stack of the frustum travers
 constexpr int kCand = 32;        // leaves processed per flush (one per lane)
 constexpr int kQueue = 3 * kCand; // per-warp queue of leaves: < kCand before a step, + up to 64 per step
 constexpr int kSchedHeader = 64;  // schedule words before the per-tile estimates
-// Per pixel tile, the BVH frontier its frustum reaches (words: count, then up to kFrontierMax node or
-// leaf entries); a count of kFrontierNone means "start at the root".  A frontier goes onto the
-// traversal stack, so it leaves room there for the traversal's own pushes (up to 64 per step; the
-// stack above a frontier peaks near 70 entries on the benchmark scene).
-constexpr int kFrontierStride = 256;
-constexpr int kFrontierMax = 160;
+// Per pixel tile, the BVH frontier its frustum reaches (kFrontierWords words: count, then up to
+// kFrontierMax node or leaf entries); a count of kFrontierNone means "start at the root".  A frontier
+// goes onto the traversal stack, so it leaves room there for the traversal's own pushes (up to 64
+// per step; the stack above a frontier peaks near 70 entries on the benchmark scene).
+constexpr int kFrontierWords = GRAY_FRONTIER_WORDS;
+constexpr int kFrontierMax = kFrontierWords - 1;
+constexpr int kFrontierSort = 256;  // sort buffer of the frontier walk (a power of two > kFrontierMax)
 constexpr uint32_t kFrontierNone = 0xFFFFFFFFu;
 constexpr int kFrontierCutDefault = 64;  // frontier nodes hold at most this many leaves
 
@@ -369,16 +370,16 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
 // One full traversal of the packet (camera rays with a common origin) with the node work spread
 // over the lanes: each step pops up to 32 nodes, one per lane, tests their child boxes against the
 // packet frustum, pushes surviving internal children and queues surviving leaves; queued leaves
-// are then intersected by every lane with its own ray (on_leaf).  With a tile frontier (front[0,
-// *nfront), *nfront >= 0) the traversal starts there instead of at the root: the frontier goes onto
-// the stack with its first entry on top, and a frontier leaf is queued when it is popped.  Returns
-// false if the shared stack overflowed (the caller then repeats the traversal per ray).
+// are then intersected by every lane with its own ray (on_leaf).  With a tile frontier (front =
+// count, entries; a count of kFrontierNone or a null front: none) the traversal starts there instead
+// of at the root: the frontier goes onto the stack with its first entry on top, and a frontier leaf
+// is queued when it is popped.  Returns false if the shared stack overflowed (the caller then
+// repeats the traversal per ray).
 template <int KB>
 __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool want,
                                                  bool first, LaneState &st, unsigned long long (*kbuf)[kFwdThreads],
                                                  const Frustum &fr, uint32_t *stk, uint32_t *cand,
-                                                 CandCache &cc, const uint32_t *front, const int *nfront,
-                                                 int32_t *status) {
+                                                 CandCache &cc, const uint32_t *front, int32_t *status) {
     const int lane = threadIdx.x & 31;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     const int n = sc.n;
@@ -389,9 +390,9 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
         on_leaf<KB>(sc, 0u, want, first, ro, rd, k, st, kbuf);
         return true;
     }
-    int sp = nfront ? *nfront : -1, nc = 0;
+    int sp = front ? (int)front[0] : -1, nc = 0;
     if (sp >= 0 && sp <= kFrontierMax) {
-        for (int i = lane; i < sp; i += 32) stk[sp - 1 - i] = front[i];
+        for (int i = lane; i < sp; i += 32) stk[sp - 1 - i] = front[1 + i];
     } else {
         if (lane == 0) stk[0] = 0u;
         sp = 1;
@@ -493,7 +494,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
                                           unsigned long long (*kbuf)[kFwdThreads], RayResult &res,
                                           const Frustum *fr = nullptr, uint32_t *wstk = nullptr,
                                           uint32_t *wcand = nullptr, CandCache *wcc = nullptr,
-                                          const uint32_t *front = nullptr, const int *nfront = nullptr) {
+                                          const uint32_t *front = nullptr) {
     const int lane = threadIdx.x & 31;
     LaneState &st = res.st;
     st.lfx = 0;
@@ -520,7 +521,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
         // ---------------- traversal ----------------
         bool per_ray = fr == nullptr;
         if (!per_ray &&
-            !traverse_frustum<KB>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, *wcc, front, nfront, status)) {
+            !traverse_frustum<KB>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, *wcc, front, status)) {
             // the frustum traversal gave up (stack overflow): discard what it gathered, trace per ray
             st.kcount = 0;
             st.ncand = 0;
@@ -759,8 +760,7 @@ struct FwdShared {
     uint32_t sstk[kWarps][kWideStack];
     uint32_t scand[kWarps][kQueue];
     CandCache scc[kWarps];
-    uint32_t front[kFrontierMax];  // the tile's BVH frontier (frontier launches)
-    int nfront;                    // its length, or -1: traversals start at the root
+    uint32_t front[kFrontierWords];  // the tile's BVH frontier (count, entries)
 };
 
 // One block's pixel tile (bx, by): 2x2 packets of tile_w x tile_h pixels, one per warp.
@@ -809,12 +809,12 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
     const bool frustum = !*a.rays_from_python && !*a.jitter;
     // the tile's frontier, read once by the block (every thread of the block gets here together)
     {
-        const uint32_t *src = a.frontier ? a.frontier + (size_t)(by * a.tiles_x + bx) * kFrontierStride : nullptr;
+        const uint32_t *src = a.frontier ? a.frontier + (size_t)(by * a.tiles_x + bx) * kFrontierWords : nullptr;
         const uint32_t cnt = src && frustum ? src[0] : kFrontierNone;
         const bool use = cnt <= (uint32_t)kFrontierMax;
         if (use)
-            for (uint32_t i = threadIdx.x; i < cnt; i += kFwdThreads) sh.front[i] = src[1 + i];
-        if (threadIdx.x == 0) sh.nfront = use ? (int)cnt : -1;
+            for (uint32_t i = threadIdx.x; i < cnt; i += kFwdThreads) sh.front[1 + i] = src[1 + i];
+        if (threadIdx.x == 0) sh.front[0] = use ? cnt : kFrontierNone;
         __syncthreads();
     }
     if (frustum) {
@@ -832,7 +832,7 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
     }
     RayResult r;
     trace_ray<KB>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sh.sstk[warp],
-                  sh.scand[warp], &sh.scc[warp], sh.front, &sh.nfront);
+                  sh.scand[warp], &sh.scc[warp], sh.front);
 
     if (!inside) return;
     if (!alive) {
@@ -909,23 +909,171 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_sched_kernel(
 // tile, not once per packet traversal).  The frontier is sorted by its boxes' centres along the
 // tile's mean direction, so packets visit it roughly front to back.  Schedule words: [0] work
 // counter, [1..33] bucket counts/cursors, [kSchedHeader, +ntiles) estimates, [kSchedHeader + ntiles,
-// +ntiles) order, then (when frontiers are on) kFrontierStride words per tile.
+// +ntiles) order, then (when frontiers are on) kFrontierWords words per tile.
 // ---------------------------------------------------------------------------------------------
 constexpr int kCostCut = 512;
 constexpr int kCostStack = 256;
 
-__global__ void __launch_bounds__(32) tile_cost_kernel(const FwdArgs a, int bw, int bh) {
-    __shared__ Frustum fr;
-    __shared__ uint32_t stk[kCostStack];
-    __shared__ float fkey[kFrontierStride];
-    __shared__ uint32_t fval[kFrontierStride];
-    const int tile = blockIdx.x, lane = threadIdx.x;
+struct FrontierScratch {
+    Frustum fr;
+    uint32_t stk[kCostStack];
+    float key[kFrontierSort];
+    uint32_t val[kFrontierSort];
+};
+
+// One warp walks the top of the BVH for a pixel rectangle whose frustum is in fs.fr: returns (on
+// every lane) the number of leaves under the frontier, the nodes of at most `cut` leaves (and the
+// leaves) it reaches; with `out`, writes the frontier there sorted front to back (count + entries),
+// or a count of kFrontierNone when the walk was cut short, the frontier does not fit or the tree is
+// malformed.  n > 1.
+__device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, uint32_t cut, FrontierScratch &fs,
+                                               uint32_t *out) {
+    const int lane = threadIdx.x & 31;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
+    const Frustum &fr = fs.fr;
+    uint32_t est = 0;
+    int nf = 0, sp = 1;
+    bool complete = true;
+    if (lane == 0) fs.stk[0] = 0u;
+    __syncwarp();
+    for (int guard = 0; sp > 0; guard++) {
+        if (guard >= 4096) {
+            complete = false;
+            break;
+        }
+        const int take = sp < 32 ? sp : 32;
+        uint32_t node = GRAY_NULL;
+        if (lane < take) node = fs.stk[sp - 1 - lane];
+        __syncwarp();
+        sp -= take;
+        // children as (a, b) = (nearer, farther) along the rectangle's mean direction, as the forward
+        uint32_t ca = 0, cb = 0;
+        bool pa = false, pb = false, bad = false;
+        float sa = 0.0f, sb = 0.0f;
+        if (node != GRAY_NULL) {
+            if (node >= (uint32_t)(n - 1)) {
+                bad = true;
+            } else {
+                const float4 q0 = nodes[4 * node], q1 = nodes[4 * node + 1], q2 = nodes[4 * node + 2],
+                             q3 = nodes[4 * node + 3];
+                const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
+                const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
+                const uint32_t c0 = __float_as_uint(q3.x), c1 = __float_as_uint(q3.y);
+                const bool p0 = frustum_box(fr, b0min, b0max), p1 = frustum_box(fr, b1min, b1max);
+                const float4 c = fr.pn[4];
+                const float s0 = fmaf(q0.z + q1.y, c.z, fmaf(q0.y + q1.x, c.y, (q0.x + q0.w) * c.x));
+                const float s1 = fmaf(q2.x + q2.w, c.z, fmaf(q1.w + q2.z, c.y, (q1.z + q2.y) * c.x));
+                const bool sw = s1 < s0;
+                ca = sw ? c1 : c0;
+                cb = sw ? c0 : c1;
+                pa = sw ? p1 : p0;
+                pb = sw ? p0 : p1;
+                sa = sw ? s1 : s0;
+                sb = sw ? s0 : s1;
+            }
+        }
+        // internal children above the cut are walked further; leaves and nodes at the cut are
+        // frontier entries
+        bool ia = false, ib = false, fa = false, fb = false;
+        if (pa) {
+            if (ca & GRAY_LEAF_BIT) {
+                fa = (ca & ~GRAY_LEAF_BIT) < (uint32_t)n;
+                bad = bad || !fa;
+                est += fa ? 1u : 0u;
+            } else if (ca < (uint32_t)(n - 1)) {
+                const uint32_t leaves = __float_as_uint(nodes[4 * ca + 3].z);
+                ia = leaves > cut;
+                fa = !ia;
+                if (fa) est += leaves;
+            } else {
+                bad = true;
+            }
+        }
+        if (pb) {
+            if (cb & GRAY_LEAF_BIT) {
+                fb = (cb & ~GRAY_LEAF_BIT) < (uint32_t)n;
+                bad = bad || !fb;
+                est += fb ? 1u : 0u;
+            } else if (cb < (uint32_t)(n - 1)) {
+                const uint32_t leaves = __float_as_uint(nodes[4 * cb + 3].z);
+                ib = leaves > cut;
+                fb = !ib;
+                if (fb) est += leaves;
+            } else {
+                bad = true;
+            }
+        }
+        // a malformed tree: leave it to the forward's own checks (root start)
+        if (__any_sync(kFull, bad)) complete = false;
+        const uint32_t ma = __ballot_sync(kFull, ia), mb = __ballot_sync(kFull, ib);
+        const int ni = __popc(ma) + __popc(mb);
+        if (sp + ni > kCostStack) {
+            complete = false;  // an estimate from what was reached is enough
+            break;
+        }
+        const int above = __popc(ma & lanemask_lt) + __popc(mb & lanemask_lt);
+        if (ia) fs.stk[sp + ni - 1 - above] = ca;
+        if (ib) fs.stk[sp + ni - 1 - above - (ia ? 1 : 0)] = cb;
+        sp += ni;
+        const uint32_t qa = __ballot_sync(kFull, fa), qb = __ballot_sync(kFull, fb);
+        const int before = nf + __popc(qa & lanemask_lt) + __popc(qb & lanemask_lt);
+        if (fa && before < kFrontierSort) {
+            fs.key[before] = sa;
+            fs.val[before] = ca;
+        }
+        if (fb && before + (fa ? 1 : 0) < kFrontierSort) {
+            fs.key[before + (fa ? 1 : 0)] = sb;
+            fs.val[before + (fa ? 1 : 0)] = cb;
+        }
+        nf += __popc(qa) + __popc(qb);
+        __syncwarp();
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) est += __shfl_xor_sync(kFull, est, off);
+    if (out) {
+        if (complete && nf <= kFrontierMax) {
+            // bitonic sort of the entries by key (padding sorts last); NaN keys compare false
+            int p2 = 32;
+            while (p2 < nf) p2 <<= 1;
+            for (int i = nf + lane; i < p2; i += 32) {
+                fs.key[i] = __int_as_float(0x7f800000);
+                fs.val[i] = GRAY_NULL;
+            }
+            __syncwarp();
+            for (int k = 2; k <= p2; k <<= 1) {
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    for (int i = lane; i < p2; i += 32) {
+                        const int ixj = i ^ j;
+                        if (ixj > i) {
+                            const float ki = fs.key[i], kj = fs.key[ixj];
+                            const bool up = (i & k) == 0;
+                            if (up ? (kj < ki) : (ki < kj)) {
+                                fs.key[i] = kj;
+                                fs.key[ixj] = ki;
+                                const uint32_t v = fs.val[i];
+                                fs.val[i] = fs.val[ixj];
+                                fs.val[ixj] = v;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+            for (int i = lane; i < nf; i += 32) out[1 + i] = fs.val[i];
+            if (lane == 0) out[0] = (uint32_t)nf;
+        } else if (lane == 0) {
+            out[0] = kFrontierNone;
+        }
+    }
+    return est;
+}
+
+__global__ void __launch_bounds__(32) tile_cost_kernel(const FwdArgs a, int bw, int bh) {
+    __shared__ FrontierScratch fs;
+    const int tile = blockIdx.x, lane = threadIdx.x;
+    uint32_t *out = a.frontier ? a.frontier + (size_t)tile * kFrontierWords : nullptr;
     uint32_t est = 0;
     const int n = a.n;
-    const uint32_t cut = a.frontier_cut > 0 ? a.frontier_cut : (uint32_t)kCostCut;
-    bool complete = false;  // the walk reached every frontier entry and they fit
-    int nf = 0;
     if (!*a.rays_from_python && !*a.jitter && !*a.render_ellipsoids && n > 1) {
         const int x0 = (tile % a.tiles_x) * bw, y0 = (tile / a.tiles_x) * bh;
         const int x1 = min(x0 + bw, (int)a.render_w) - 1, y1 = min(y0 + bh, (int)a.render_h) - 1;
@@ -935,142 +1083,12 @@ __global__ void __launch_bounds__(32) tile_cost_kernel(const FwdArgs a, int bw, 
                              camera_ray(a.w2c, *a.fov, x1, y0, a.render_w, a.render_h, 0.0f, 0.0f),
                              camera_ray(a.w2c, *a.fov, x1, y1, a.render_w, a.render_h, 0.0f, 0.0f),
                              camera_ray(a.w2c, *a.fov, x0, y1, a.render_w, a.render_h, 0.0f, 0.0f)};
-            make_frustum(fr, o, d, a.root_box);
-            stk[0] = 0u;
+            make_frustum(fs.fr, o, d, a.root_box);
         }
         __syncwarp();
-        int sp = 1;
-        complete = true;
-        for (int guard = 0; sp > 0; guard++) {
-            if (guard >= 4096) {
-                complete = false;
-                break;
-            }
-            const int take = sp < 32 ? sp : 32;
-            uint32_t node = GRAY_NULL;
-            if (lane < take) node = stk[sp - 1 - lane];
-            __syncwarp();
-            sp -= take;
-            // children as (a, b) = (nearer, farther) along the tile's mean direction, as the forward
-            uint32_t ca = 0, cb = 0;
-            bool pa = false, pb = false, bad = false;
-            float sa = 0.0f, sb = 0.0f;
-            if (node != GRAY_NULL) {
-                if (node >= (uint32_t)(n - 1)) {
-                    bad = true;
-                } else {
-                    const float4 q0 = a.nodes[4 * node], q1 = a.nodes[4 * node + 1], q2 = a.nodes[4 * node + 2],
-                                 q3 = a.nodes[4 * node + 3];
-                    const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
-                    const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
-                    const uint32_t c0 = __float_as_uint(q3.x), c1 = __float_as_uint(q3.y);
-                    const bool p0 = frustum_box(fr, b0min, b0max), p1 = frustum_box(fr, b1min, b1max);
-                    const float4 c = fr.pn[4];
-                    const float s0 = fmaf(q0.z + q1.y, c.z, fmaf(q0.y + q1.x, c.y, (q0.x + q0.w) * c.x));
-                    const float s1 = fmaf(q2.x + q2.w, c.z, fmaf(q1.w + q2.z, c.y, (q1.z + q2.y) * c.x));
-                    const bool sw = s1 < s0;
-                    ca = sw ? c1 : c0;
-                    cb = sw ? c0 : c1;
-                    pa = sw ? p1 : p0;
-                    pb = sw ? p0 : p1;
-                    sa = sw ? s1 : s0;
-                    sb = sw ? s0 : s1;
-                }
-            }
-            // internal children above the cut are walked further; leaves and nodes at the cut are
-            // frontier entries
-            bool ia = false, ib = false, fa = false, fb = false;
-            if (pa) {
-                if (ca & GRAY_LEAF_BIT) {
-                    fa = (ca & ~GRAY_LEAF_BIT) < (uint32_t)n;
-                    bad = bad || !fa;
-                    est += fa ? 1u : 0u;
-                } else if (ca < (uint32_t)(n - 1)) {
-                    const uint32_t leaves = __float_as_uint(a.nodes[4 * ca + 3].z);
-                    ia = leaves > cut;
-                    fa = !ia;
-                    if (fa) est += leaves;
-                } else {
-                    bad = true;
-                }
-            }
-            if (pb) {
-                if (cb & GRAY_LEAF_BIT) {
-                    fb = (cb & ~GRAY_LEAF_BIT) < (uint32_t)n;
-                    bad = bad || !fb;
-                    est += fb ? 1u : 0u;
-                } else if (cb < (uint32_t)(n - 1)) {
-                    const uint32_t leaves = __float_as_uint(a.nodes[4 * cb + 3].z);
-                    ib = leaves > cut;
-                    fb = !ib;
-                    if (fb) est += leaves;
-                } else {
-                    bad = true;
-                }
-            }
-            // a malformed tree: leave it to the forward's own checks (root start)
-            if (__any_sync(kFull, bad)) complete = false;
-            const uint32_t ma = __ballot_sync(kFull, ia), mb = __ballot_sync(kFull, ib);
-            const int ni = __popc(ma) + __popc(mb);
-            if (sp + ni > kCostStack) {
-                complete = false;  // an estimate from what was reached is enough
-                break;
-            }
-            const int above = __popc(ma & lanemask_lt) + __popc(mb & lanemask_lt);
-            if (ia) stk[sp + ni - 1 - above] = ca;
-            if (ib) stk[sp + ni - 1 - above - (ia ? 1 : 0)] = cb;
-            sp += ni;
-            const uint32_t qa = __ballot_sync(kFull, fa), qb = __ballot_sync(kFull, fb);
-            const int before = nf + __popc(qa & lanemask_lt) + __popc(qb & lanemask_lt);
-            if (fa && before < kFrontierStride - 1) {
-                fkey[before] = sa;
-                fval[before] = ca;
-            }
-            if (fb && before + (fa ? 1 : 0) < kFrontierStride - 1) {
-                fkey[before + (fa ? 1 : 0)] = sb;
-                fval[before + (fa ? 1 : 0)] = cb;
-            }
-            nf += __popc(qa) + __popc(qb);
-            __syncwarp();
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) est += __shfl_xor_sync(kFull, est, off);
-    }
-    if (a.frontier) {
-        uint32_t *out = a.frontier + (size_t)tile * kFrontierStride;
-        if (complete && nf <= kFrontierMax) {
-            // bitonic sort of the entries by key (padding sorts last); NaN keys compare false
-            int p2 = 32;
-            while (p2 < nf) p2 <<= 1;
-            for (int i = nf + lane; i < p2; i += 32) {
-                fkey[i] = __int_as_float(0x7f800000);
-                fval[i] = GRAY_NULL;
-            }
-            __syncwarp();
-            for (int k = 2; k <= p2; k <<= 1) {
-                for (int j = k >> 1; j > 0; j >>= 1) {
-                    for (int i = lane; i < p2; i += 32) {
-                        const int ixj = i ^ j;
-                        if (ixj > i) {
-                            const float ki = fkey[i], kj = fkey[ixj];
-                            const bool up = (i & k) == 0;
-                            if (up ? (kj < ki) : (ki < kj)) {
-                                fkey[i] = kj;
-                                fkey[ixj] = ki;
-                                const uint32_t v = fval[i];
-                                fval[i] = fval[ixj];
-                                fval[ixj] = v;
-                            }
-                        }
-                    }
-                    __syncwarp();
-                }
-            }
-            for (int i = lane; i < nf; i += 32) out[1 + i] = fval[i];
-            if (lane == 0) out[0] = (uint32_t)nf;
-        } else if (lane == 0) {
-            out[0] = kFrontierNone;
-        }
+        est = frontier_walk(a.nodes, n, a.frontier_cut > 0 ? a.frontier_cut : (uint32_t)kCostCut, fs, out);
+    } else if (out && lane == 0) {
+        out[0] = kFrontierNone;
     }
     if (lane == 0) {
         a.schedule[kSchedHeader + tile] = est;
@@ -1275,12 +1293,54 @@ __global__ void __launch_bounds__(kEllTileX * kEllTileY) ellipsoid_kernel(const 
 // Batched render: many views (of one or several resident scenes) in one persistent launch.
 // Warps pull 32-ray packets from a global counter; packet -> (view, tile) through the views'
 // packet offsets.  Forward only (no gradients, no hit lists); per view the output is RGB.
+// A view's packets form groups of 2x2 (group_offset numbers them across views); with a frontier
+// buffer, batch_frontier_kernel first writes each group's BVH frontier and the packets of the group
+// start their traversals there, as the plain forward's blocks do.
 // ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ int batch_view_of(const gray_batch_view *views, int nviews, uint32_t packet) {
+    int v = 0;
+    while (v + 1 < nviews && views[v + 1].packet_offset <= packet) v++;
+    return v;
+}
+
+__global__ void __launch_bounds__(32) batch_frontier_kernel(const gray_batch_scene *__restrict__ scenes,
+                                                            const gray_batch_view *__restrict__ views, int nviews,
+                                                            uint32_t *__restrict__ frontier, int tile_w,
+                                                            uint32_t cut) {
+    __shared__ FrontierScratch fs;
+    const uint32_t group = blockIdx.x;
+    const int lane = threadIdx.x;
+    int v = 0;
+    while (v + 1 < nviews && views[v + 1].group_offset <= group) v++;
+    const gray_batch_view &vw = views[v];
+    const gray_batch_scene &bs = scenes[vw.scene];
+    uint32_t *out = frontier + (size_t)group * kFrontierWords;
+    const int tile_h = 32 / tile_w;
+    const uint32_t tiles_x = (vw.width + tile_w - 1) / tile_w;
+    const uint32_t gxn = (tiles_x + 1) / 2, local = group - vw.group_offset;
+    const int x0 = (int)((local % gxn) * 2 * tile_w), y0 = (int)((local / gxn) * 2 * tile_h);
+    if (bs.n <= 1 || x0 >= (int)vw.width || y0 >= (int)vw.height) {
+        if (lane == 0) out[0] = kFrontierNone;
+        return;
+    }
+    const int x1 = min(x0 + 2 * tile_w, (int)vw.width) - 1, y1 = min(y0 + 2 * tile_h, (int)vw.height) - 1;
+    if (lane == 0) {
+        const f3 o = mk3(vw.origin[0], vw.origin[1], vw.origin[2]);
+        const f3 d[4] = {camera_ray(vw.w2c, vw.fov_y, x0, y0, vw.width, vw.height, 0.0f, 0.0f),
+                         camera_ray(vw.w2c, vw.fov_y, x1, y0, vw.width, vw.height, 0.0f, 0.0f),
+                         camera_ray(vw.w2c, vw.fov_y, x1, y1, vw.width, vw.height, 0.0f, 0.0f),
+                         camera_ray(vw.w2c, vw.fov_y, x0, y1, vw.width, vw.height, 0.0f, 0.0f)};
+        make_frustum(fs.fr, o, d, bs.root_box);
+    }
+    __syncwarp();
+    frontier_walk(reinterpret_cast<const float4 *>(bs.nodes), bs.n, cut, fs, out);
+}
+
 template <int KB, int MINB>
 __global__ void __launch_bounds__(kFwdThreads, MINB)
     trace_batch_kernel(const gray_batch_scene *__restrict__ scenes, const gray_batch_view *__restrict__ views,
                        int nviews, uint32_t total_packets, float *__restrict__ out, uint32_t *__restrict__ counter,
-                       int tile_w, int32_t *status) {
+                       int tile_w, const uint32_t *__restrict__ frontier, int32_t *status) {
     __shared__ unsigned long long kbuf[KB][kFwdThreads];
     __shared__ Frustum sfr[kWarps];
     __shared__ uint32_t sstk[kWarps][kWideStack];
@@ -1298,9 +1358,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
         if (lane == 0) packet = atomicAdd(counter, 1u);
         packet = __shfl_sync(kFull, packet, 0);
         if (packet >= total_packets) break;
-        int v = 0;
-        while (v + 1 < nviews && views[v + 1].packet_offset <= packet) v++;
-        const gray_batch_view &vw = views[v];
+        const gray_batch_view &vw = views[batch_view_of(views, nviews, packet)];
         const gray_batch_scene &bs = scenes[vw.scene];
         const uint32_t local = packet - vw.packet_offset;
         const uint32_t tiles_x = (vw.width + tile_w - 1) / tile_w;
@@ -1336,9 +1394,14 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
             make_frustum(sfr[warp], ro, d, s_sc[warp].root_box);
         }
         __syncwarp();
+        const uint32_t *front = nullptr;
+        if (frontier) {
+            const uint32_t tx = local % tiles_x, ty = local / tiles_x;
+            front = frontier + (size_t)(vw.group_offset + (ty / 2) * ((tiles_x + 1) / 2) + tx / 2) * kFrontierWords;
+        }
         RayResult r;
         trace_ray<KB>(sc, k, ro, rd, inside, false, hs, status, kbuf, r, &sfr[warp], sstk[warp], scand[warp],
-                      &scc[warp]);
+                      &scc[warp], front);
         if (!inside) continue;
         float r0, r1, r2;
         finish_ray(r, bs.bg, 1e-12f, false, r0, r1, r2);
@@ -1440,7 +1503,7 @@ cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_
         // densest tiles first: estimate, bucket, then a persistent grid that takes tiles in order
         a.schedule = p.hitlist.schedule;
         a.frontier_cut = fcut == 0 ? kFrontierCutDefault : fcut == 1 ? 32u : fcut == 2 ? 128u : 0u;
-        if (a.frontier_cut > 0 && (size_t)a.ntiles <= (words - kSchedHeader) / (2 + kFrontierStride))
+        if (a.frontier_cut > 0 && (size_t)a.ntiles <= (words - kSchedHeader) / (2 + kFrontierWords))
             a.frontier = a.schedule + kSchedHeader + 2 * (size_t)a.ntiles;
         if ((e = cudaMemsetAsync(a.schedule, 0, sizeof(uint32_t) * kSchedHeader, s)) != cudaSuccess) return e;
         tile_cost_kernel<<<a.ntiles, 32, 0, s>>>(a, bw, bh);
@@ -1465,25 +1528,35 @@ size_t gray_schedule_words_for(uint32_t width, uint32_t height) {
     const size_t t8 = (size_t)((width + 7) / 8) * (size_t)((height + 7) / 8);
     const size_t ta = (size_t)((width + 7) / 8) * (size_t)((height + 15) / 16);
     const size_t tb = (size_t)((width + 15) / 16) * (size_t)((height + 7) / 8);
-    return (size_t)kSchedHeader + 2 * t8 + (ta > tb ? ta : tb) * kFrontierStride;
+    return (size_t)kSchedHeader + 2 * t8 + (ta > tb ? ta : tb) * kFrontierWords;
 }
 
 cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int nviews,
-                               uint32_t total_packets, float *out, uint32_t *counter, int variant, int blocks_per_sm,
-                               int32_t *status, cudaStream_t s) {
+                               uint32_t total_packets, float *out, uint32_t *counter, uint32_t *frontier,
+                               uint32_t total_groups, int variant, int blocks_per_sm, int32_t *status,
+                               cudaStream_t s) {
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     const int v = variant > 0 ? variant : kDefaultTraceVariant;
     const int tile_w = (v & 4) ? 4 : 8;
+    const int fcut = (v >> 3) & 3;
+    const uint32_t cut = fcut == 0 ? kFrontierCutDefault : fcut == 1 ? 32u : fcut == 2 ? 128u : 0u;
     const unsigned int grid = (unsigned int)(sms * (blocks_per_sm > 0 ? blocks_per_sm : 4));
     if ((e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
+    if (!frontier || cut == 0 || total_groups == 0) {
+        frontier = nullptr;
+    } else {
+        batch_frontier_kernel<<<total_groups, 32, 0, s>>>(scenes, views, nviews, frontier, tile_w, cut);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    const uint32_t *fr = frontier;
     switch (v & 3) {
-        case 0: trace_batch_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
-        case 1: trace_batch_kernel<32, 4><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
-        case 2: trace_batch_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
-        default: trace_batch_kernel<16, 6><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, status); break;
+        case 0: trace_batch_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, status); break;
+        case 1: trace_batch_kernel<32, 4><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, status); break;
+        case 2: trace_batch_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, status); break;
+        default: trace_batch_kernel<16, 6><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, status); break;
     }
     return cudaGetLastError();
 }

@@ -24,7 +24,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
-from .batch import DEFAULT_BLOCKS_PER_SM, DEFAULT_VARIANT, BatchRenderer
+from .batch import DEFAULT_BLOCKS_PER_SM, DEFAULT_VARIANT, BatchRenderer, _bind
 from .camera import CameraInfo
 
 
@@ -94,8 +94,12 @@ class RenderServer:
         return r
 
     def _request_bytes(self, r: Request) -> int:
+        """Output image, the view's colour buffer and its packet groups' BVH frontiers (at most one
+        group per 128 pixels, rounded up per 8x16 or 16x8 pixel group)."""
         n = self.tracers[r.scene].get_gaussians().count
-        return 3 * 4 * r.rays + 12 * n + 256
+        w, h = r.camera.image_width, r.camera.image_height
+        groups = max(-(-w // 8) * -(-h // 16), -(-w // 16) * -(-h // 8))
+        return 3 * 4 * r.rays + 12 * n + 4 * int(_bind().gray_frontier_words()) * groups + 256
 
     def _retire(self):
         now = time.perf_counter()

@@ -192,7 +192,7 @@ typedef struct gray_batch_view {
     uint32_t width, height;
     uint32_t scene;        /* index into the scene table */
     uint32_t packet_offset;/* first packet of this view; views in increasing order */
-    uint32_t pad;
+    uint32_t group_offset; /* first frontier group of this view (gray_batch_groups); increasing */
     uint64_t out_offset;   /* float index of pixel (0,0): RGB, row-major, width x height */
     const float *channels; /* [n,3] colours of the view's scene for this view (gray_batch_prep) */
 } gray_batch_view;
@@ -200,17 +200,26 @@ typedef struct gray_batch_view {
 /* Packets (32-ray tiles) of a width x height view for a kernel variant. */
 uint32_t gray_batch_packets(uint32_t width, uint32_t height, int32_t variant);
 
+/* Frontier groups (2x2 packets) of a width x height view for a kernel variant; a batch's frontier
+ * buffer holds GRAY_FRONTIER_WORDS words per group of all its views. */
+uint32_t gray_batch_groups(uint32_t width, uint32_t height, int32_t variant);
+#define GRAY_FRONTIER_WORDS 161
+uint32_t gray_frontier_words(void);
+
 /* Per-view colours of one scene: live values (as forward_pass_display) and, when enable_sh, the SH
  * colour of every Gaussian for each of the nviews camera origins (device [nviews,3]) into
  * channels_out (device [nviews,n,3]); without SH the scene's channels are copied per view. */
 int gray_batch_prep(const gray_params *p, const float *origins, int32_t nviews, float *channels_out, void *stream);
 
 /* Render the views (device arrays scenes[], views[]) into out; work_counter is one device word
- * the launch resets and consumes; variant as gray_params.trace_variant; blocks_per_sm sizes the
- * persistent grid (0 = 4). */
+ * the launch resets and consumes; frontier is a device workspace of total_groups *
+ * GRAY_FRONTIER_WORDS words (NULL: every traversal starts at the root) into which the launch first
+ * writes each packet group's BVH frontier; variant as gray_params.trace_variant; blocks_per_sm
+ * sizes the persistent grid (0 = 4). */
 int gray_render_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int32_t nviews,
-                      uint32_t total_packets, float *out, uint32_t *work_counter, int32_t variant,
-                      int32_t blocks_per_sm, int32_t *status, void *stream);
+                      uint32_t total_packets, float *out, uint32_t *work_counter, uint32_t *frontier,
+                      uint32_t total_groups, int32_t variant, int32_t blocks_per_sm, int32_t *status,
+                      void *stream);
 
 /* Workspace sizes in 32-bit words for n Gaussians: sort_tmp_words. */
 size_t gray_sort_tmp_words(int32_t n);

@@ -289,9 +289,12 @@ def test_hitlist_overflow_is_reported_not_trapped(oracle):
     assert torch.isfinite(rt.get_framebuffer().output_channels).all()
 
 
-def test_adam_step_bit_exact(oracle):
+@pytest.mark.parametrize("n,laziness,update_channels", [(1037, 1, False), (40009, 2, True), (40009, 1, False)])
+def test_adam_step_bit_exact(oracle, n, laziness, update_channels):
+    """Fused Adam against the oracle: ragged group lengths, more work units than the persistent grid
+    holds (40k Gaussians), the SH groups skipped when the step is not a multiple of the laziness, and
+    the channels group either updated or only zeroed."""
     rng = np.random.default_rng(4)
-    n = 1037
     rt = G.make_tracer(8, 8, rng.normal(0, 1, (n, 3)), rng.normal(0, 1, (n, 4)), rng.normal(-3, 0.3, (n, 3)),
                        rng.normal(0, 1, (n, 1)), sh_dc=rng.normal(0.5, 0.2, (n, 1, 3)),
                        sh_rest=rng.normal(0, 0.05, (n, 15, 3)), sh_degree=3)
@@ -315,17 +318,19 @@ def test_adam_step_bit_exact(oracle):
             st["v_" + name] = getattr(g, "second_moment_" + t).cpu().numpy().reshape(-1).copy()
     cfg = rt.get_config()
     cfg.zero_grads.fill_(True)
-    cfg.update_channels.fill_(False)
+    cfg.update_channels.fill_(update_channels)
+    g.sh_update_laziness.fill_(laziness)
     rt.get_metadata().total_num_steps.fill_(6)
     rt.step()  # step becomes 7
     torch.cuda.synchronize()
-    oracle.adam_step(st, lrs, n, 15, 7, zero_grads=True, update_channels=False)
+    oracle.adam_step(st, lrs, n, 15, 7, zero_grads=True, update_channels=update_channels, laziness=laziness)
     for name in ("channels", "opacity", "mean", "rotation", "scale", "sh_dc", "sh_rest"):
         t = name_map.get(name, name)
         assert np.array_equal(getattr(g, t).detach().cpu().numpy().reshape(-1), st[name]), name
         assert np.array_equal(getattr(g, "first_moment_" + t).cpu().numpy().reshape(-1), st["m_" + name]), name
         assert np.array_equal(getattr(g, "second_moment_" + t).cpu().numpy().reshape(-1), st["v_" + name]), name
-        assert not getattr(g, "grad_" + t).any()
+        assert np.array_equal(getattr(g, "grad_" + t).cpu().numpy().reshape(-1), st["g_" + name]), name
+    assert not g.grad_mean.any()  # zeroed after the update
     assert int(rt.get_metadata().total_num_steps.item()) == 7
 
 
