@@ -36,7 +36,7 @@ LR = dict(mean=1.6e-4, scale=5e-3, rotation=1e-3, opacity=2.5e-2, sh=2.5e-3)
 
 
 def parse():
-    return parse_args(None)
+    return apply_scene(parse_args(None))
 
 
 def parse_args(argv):
@@ -54,25 +54,49 @@ def parse_args(argv):
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--no-served", action="store_true", help="skip the served measurement only")
     ap.add_argument("--trace-variant", type=int, default=0, help="forward-kernel variant (0 = library default)")
+    ap.add_argument("--scene", default="clustered", choices=["clustered", "small", "gradcheck"],
+                    help="clustered: --n-gaussians clustered Gaussians on a radius-8 orbit; small: 64 Gaussians in "
+                         "[-1,1]^3, 256x256 camera at distance 4 (fx = 256); gradcheck: 1000 Gaussians in [-2,2]^3, "
+                         "128x128 camera")
     return ap.parse_args(argv)
 
 
+def apply_scene(a):
+    """The small and gradcheck scenes fix their own size and resolution."""
+    if a.scene == "small":
+        a.n_gaussians, a.width, a.height = 64, 256, 256
+    elif a.scene == "gradcheck":
+        a.n_gaussians, a.width, a.height = 1000, 128, 128
+    return a
+
+
 def workload_config(a, rank=0):
-    return {"workload": f"train step, {a.n_gaussians / 1e6:g}M clustered Gaussians, {a.width}x{a.height}",
+    kind = {"clustered": "clustered", "small": "uniform [-1,1]^3", "gradcheck": "uniform [-2,2]^3"}[a.scene]
+    count = f"{a.n_gaussians / 1e6:g}M" if a.n_gaussians >= 100_000 else f"{a.n_gaussians}"
+    return {"workload": f"train step, {count} {kind} Gaussians, {a.width}x{a.height}",
             "n_gaussians": a.n_gaussians, "width": a.width, "height": a.height, "rays_per_step": a.width * a.height,
             "sh_degree": 3, "t_threshold": 0.03, "alpha_threshold": 0.01, "exp_power": 2.0,
-            "l2": "inputs larger than L2 (no flush)", "seed": 0}
+            "l2": "inputs larger than L2 (no flush)" if a.scene == "clustered" and a.n_gaussians >= 1_000_000
+            else "inputs smaller than L2, resident between steps (no flush)", "seed": 0}
 
 
 def make_scene(a):
     from gray_gb300 import synthetic
 
+    if a.scene == "small":
+        return synthetic.small_scene(seed=0)
+    if a.scene == "gradcheck":
+        return synthetic.gradcheck_scene(seed=0)
     return synthetic.clustered_scene(a.n_gaussians, seed=0)
 
 
 def make_camera(a, rank):
     from gray_gb300 import synthetic
 
+    if a.scene == "small":
+        return synthetic.camera_small(a.width, a.height)
+    if a.scene == "gradcheck":
+        return synthetic.camera_small(a.width, a.height, focal=float(a.width))
     return synthetic.orbit_camera(0.3 + 0.7 * rank, a.width, a.height)
 
 
@@ -321,7 +345,7 @@ def gpu_arm(a, rank, world, local_rank):
 
     line = {"metric": METRIC, "value": round(steps_per_s, 3), "unit": "train-steps/s", "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered scene)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded {a.scene} scene)",
             "config": dict(workload_config(a), parallelism=f"replicas x{world}"),
             "rays_per_s": round(rays_per_s, 1), "train_rays_per_s": round(R * steps_per_s, 1),
             "e2e": {"value": round(e2e_steps_per_s, 3), "unit": "train-steps/s",
@@ -517,7 +541,7 @@ def reference_arm(a, rank, world):
     v = round(1.0 / t, 5)
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "train-steps/s", "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1000 * t, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered scene)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded {a.scene} scene)",
             "config": dict(workload_config(a), parallelism="cpu"),
             "cpu_baseline": {"value": v, "unit": "train-steps/s", "cores": cs.threads, "kind": "port",
                              "sample": f"per step {cs.ro.shape[0]} rays forward+backward + 200k-Gaussian slice, "
