@@ -238,9 +238,11 @@ __global__ void karras_kernel(int n, const uint32_t *__restrict__ codes, const u
         c1 = (uint32_t)(gamma + 1);
         int_parent[gamma + 1] = i;
     }
-    // word 14: number of leaves below the node (the forward's work estimate reads it)
+    // words 14 and 15: leaves below the node and below its first child (the forward's frontier
+    // walk reads them)
     float4 *nd = reinterpret_cast<float4 *>(nodes) + 4 * (size_t)i;
-    nd[3] = make_float4(__uint_as_float(c0), __uint_as_float(c1), __uint_as_float((uint32_t)(hi_i - lo_i + 1)), 0.0f);
+    nd[3] = make_float4(__uint_as_float(c0), __uint_as_float(c1), __uint_as_float((uint32_t)(hi_i - lo_i + 1)),
+                        __uint_as_float((uint32_t)(gamma - lo_i + 1)));
     if (i == 0) int_parent[0] = -1;
 }
 

@@ -947,7 +947,7 @@ __device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, ui
         __syncwarp();
         sp -= take;
         // children as (a, b) = (nearer, farther) along the rectangle's mean direction, as the forward
-        uint32_t ca = 0, cb = 0;
+        uint32_t ca = 0, cb = 0, la = 0, lb = 0;  // children and the leaves below them
         bool pa = false, pb = false, bad = false;
         float sa = 0.0f, sb = 0.0f;
         if (node != GRAY_NULL) {
@@ -959,6 +959,7 @@ __device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, ui
                 const float b0min[3] = {q0.x, q0.y, q0.z}, b0max[3] = {q0.w, q1.x, q1.y};
                 const float b1min[3] = {q1.z, q1.w, q2.x}, b1max[3] = {q2.y, q2.z, q2.w};
                 const uint32_t c0 = __float_as_uint(q3.x), c1 = __float_as_uint(q3.y);
+                const uint32_t l0 = __float_as_uint(q3.w), l1 = __float_as_uint(q3.z) - l0;
                 const bool p0 = frustum_box(fr, b0min, b0max), p1 = frustum_box(fr, b1min, b1max);
                 const float4 c = fr.pn[4];
                 const float s0 = fmaf(q0.z + q1.y, c.z, fmaf(q0.y + q1.x, c.y, (q0.x + q0.w) * c.x));
@@ -970,6 +971,8 @@ __device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, ui
                 pb = sw ? p0 : p1;
                 sa = sw ? s1 : s0;
                 sb = sw ? s0 : s1;
+                la = sw ? l1 : l0;
+                lb = sw ? l0 : l1;
             }
         }
         // internal children above the cut are walked further; leaves and nodes at the cut are
@@ -981,10 +984,9 @@ __device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, ui
                 bad = bad || !fa;
                 est += fa ? 1u : 0u;
             } else if (ca < (uint32_t)(n - 1)) {
-                const uint32_t leaves = __float_as_uint(nodes[4 * ca + 3].z);
-                ia = leaves > cut;
+                ia = la > cut;
                 fa = !ia;
-                if (fa) est += leaves;
+                if (fa) est += la;
             } else {
                 bad = true;
             }
@@ -995,10 +997,9 @@ __device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, ui
                 bad = bad || !fb;
                 est += fb ? 1u : 0u;
             } else if (cb < (uint32_t)(n - 1)) {
-                const uint32_t leaves = __float_as_uint(nodes[4 * cb + 3].z);
-                ib = leaves > cut;
+                ib = lb > cut;
                 fb = !ib;
-                if (fb) est += leaves;
+                if (fb) est += lb;
             } else {
                 bad = true;
             }

@@ -533,9 +533,11 @@ void orc_lbvh_build(int n, const float *aabb, const uint8_t *visible, orc_bvh *o
         }
         float *nd = out->nodes + 16 * (size_t)i;
         uint32_t leaves = (uint32_t)(hi_i - lo_i + 1); /* word 14: leaves below the node */
+        uint32_t leaves0 = (uint32_t)(gamma - lo_i + 1); /* word 15: leaves below child 0 */
         memcpy(nd + 12, &c0, 4);
         memcpy(nd + 13, &c1, 4);
         memcpy(nd + 14, &leaves, 4);
+        memcpy(nd + 15, &leaves0, 4);
     }
     orc_lbvh_refit(out, aabb);
 }
