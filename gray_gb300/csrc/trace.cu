@@ -1582,25 +1582,35 @@ __device__ __forceinline__ void red_add4(float *addr, float x, float y, float z,
 }
 
 // Adds one hit's 16 gradient values to the Gaussian's accumulator row.  Neighbouring pixels
-// composite the same Gaussians at the same replay step, and vector reductions on one row serialise
-// in L2, so the lanes of the warp that hold the same Gaussian first combine their values with
-// shuffles and the lowest of them issues the four reductions.
+// composite the same Gaussians at the same replay step (on the benchmark scene a warp's lanes form
+// groups of 16 on average, often the whole warp), and vector reductions on one row serialise in L2,
+// so the lanes that hold the same Gaussian first combine their values and the lowest of them issues
+// the four reductions.  The combination is a tree over the group's ranks: every lane knows the next
+// member of its group (`nxt`, the member `s` ranks further after the round of stride s, found by
+// pointer jumping), and in the round of stride s the members whose rank is a multiple of 2s add
+// the partial sum of the member s ranks further; after ceil(log2(largest group)) rounds the lowest
+// member holds the group's sum (16 shuffles per round instead of 16 per member).
 __device__ __forceinline__ void reduce_hit(float *row, uint32_t gid, float (&v)[16]) {
     const unsigned active = __activemask();
     const unsigned grp = __match_any_sync(active, gid);
     const int lane = threadIdx.x & 31;
-    const int leader = __ffs(grp) - 1;
-    unsigned rest = grp & ~(1u << leader);
-    while (rest) {
-        const int src = __ffs(rest) - 1;
-        rest &= rest - 1;
+    const unsigned below = (1u << lane) - 1u;
+    const int rank = __popc(grp & below);
+    const int gmax = (int)__reduce_max_sync(active, (unsigned)__popc(grp));
+    const unsigned above = grp & ~below & ~(1u << lane);
+    int nxt = above ? __ffs(above) - 1 : -1;  // the member one rank further, -1: none
+    for (int s = 1; s < gmax; s <<= 1) {
+        const int src = nxt >= 0 ? nxt : lane;
+        const bool take = nxt >= 0 && (rank & (2 * s - 1)) == 0;
 #pragma unroll
         for (int k = 0; k < 16; k++) {
-            const float t = __shfl_sync(grp, v[k], src);
-            if (lane == leader) v[k] += t;
+            const float t = __shfl_sync(active, v[k], src);
+            if (take) v[k] += t;
         }
+        const int jump = __shfl_sync(active, nxt, src);
+        nxt = nxt >= 0 ? jump : -1;
     }
-    if (lane == leader) {
+    if (rank == 0) {
         red_add4(row, v[0], v[1], v[2], v[3]);
         red_add4(row + 4, v[4], v[5], v[6], v[7]);
         red_add4(row + 8, v[8], v[9], v[10], v[11]);
