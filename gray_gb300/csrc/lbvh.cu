@@ -316,17 +316,138 @@ __global__ void refit_kernel(int n, const float4 *__restrict__ aabb, const uint3
     }
 }
 
+__device__ __forceinline__ void write_root_box(float *root_box, const float box[6]) {
+    root_box[0] = box[0];
+    root_box[1] = box[1];
+    root_box[2] = box[2];
+    root_box[3] = 0.0f;
+    root_box[4] = box[3];
+    root_box[5] = box[4];
+    root_box[6] = box[5];
+    root_box[7] = 0.0f;
+}
+
+// Two-phase refit.  Phase 1: a block takes kThreads consecutive sorted leaves and climbs, as
+// refit_kernel does, through the internal nodes whose leaf range lies inside the block's (a Karras
+// node's index is one end of its range, so a local node's index is inside the block too): visit
+// counters and the sibling's box are in shared memory, so most of the tree is built without a
+// global atomic.  A climber tracks its subtree's leaf range [lo, hi]; a parent reached through
+// child 0 covers [lo, lo + leaves - 1], through child 1 [hi - leaves + 1, hi].  At the first node
+// whose range crosses the block's edge the climber stores its box and counts its visit in global
+// memory; the second arriver there appends the node to a queue (at most one node per block
+// boundary: the one that splits it) instead of climbing on, so no block stays resident for a long
+// climb.  Phase 2: one thread per queued node climbs the rest of the tree with the global protocol.
+// Boxes are min/max unions, so the result does not depend on the order of the work.
+__global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const float4 *__restrict__ aabb,
+                                                               const uint32_t *__restrict__ order,
+                                                               const int32_t *__restrict__ leaf_parent,
+                                                               const int32_t *__restrict__ int_parent,
+                                                               float *__restrict__ nodes, uint32_t *__restrict__ flags,
+                                                               uint32_t *__restrict__ queue, float *__restrict__ root_box) {
+    __shared__ uint32_t sflag[kThreads];
+    __shared__ float sbox[kThreads][12];
+    const int base = blockIdx.x * kThreads;
+    sflag[threadIdx.x] = 0u;
+    __syncthreads();
+    const int k = base + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t gid = order[k];
+    const float4 a = aabb[2 * gid], b = aabb[2 * gid + 1];
+    float box[6] = {a.x, a.y, a.z, b.x, b.y, b.z};
+    int p = n > 1 ? leaf_parent[k] : -1;
+    if (p < 0) {
+        write_root_box(root_box, box);
+        return;
+    }
+    int lo = k, hi = k;
+    uint32_t link = gid | GRAY_LEAF_BIT;
+    for (int guard = 0; guard < 128; guard++) {
+        const float4 q3 = __ldcg(reinterpret_cast<const float4 *>(nodes) + 4 * (size_t)p + 3);
+        const int slot = __float_as_uint(q3.x) == link ? 0 : 1;
+        const int leaves = (int)__float_as_uint(q3.z);
+        const int plo = slot == 0 ? lo : hi - leaves + 1, phi = slot == 0 ? lo + leaves - 1 : hi;
+        store_child_box(nodes, p, slot, box);
+        if (plo < base || phi >= base + kThreads) {
+            // the parent's range leaves the block: global counter, then phase 2
+            if (add_acq_rel(&flags[p], 1u) == 0u) return;
+            const uint32_t at = atomicAdd(queue, 1u);
+            queue[1 + at] = (uint32_t)p;
+            return;
+        }
+        float *sb = sbox[p - base];
+#pragma unroll
+        for (int q = 0; q < 6; q++) sb[6 * slot + q] = box[q];
+        __threadfence_block();
+        if (atomicAdd(&sflag[p - base], 1u) == 0u) return;
+        __threadfence_block();
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            box[q] = fminf(box[q], sb[6 * (1 - slot) + q]);
+            box[3 + q] = fmaxf(box[3 + q], sb[6 * (1 - slot) + 3 + q]);
+        }
+        lo = plo;
+        hi = phi;
+        link = (uint32_t)p;
+        p = int_parent[p];
+        if (p < 0) {
+            write_root_box(root_box, box);
+            return;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) refit_top_kernel(const int32_t *__restrict__ int_parent,
+                                                             float *__restrict__ nodes, uint32_t *__restrict__ flags,
+                                                             const uint32_t *__restrict__ queue,
+                                                             float *__restrict__ root_box) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= queue[0]) return;
+    int p = (int)queue[1 + i];
+    for (int guard = 0; guard < 128; guard++) {
+        // both child boxes of p are complete
+        const float *nd = nodes + 16 * (size_t)p;
+        float box[6];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            box[q] = fminf(__ldcg(nd + q), __ldcg(nd + 6 + q));
+            box[3 + q] = fmaxf(__ldcg(nd + 3 + q), __ldcg(nd + 9 + q));
+        }
+        const int pp = int_parent[p];
+        if (pp < 0) {
+            write_root_box(root_box, box);
+            return;
+        }
+        const uint32_t c0 = __float_as_uint(__ldcg(nodes + 16 * (size_t)pp + 12));
+        store_child_box(nodes, pp, c0 == (uint32_t)p ? 0 : 1, box);
+        if (add_acq_rel(&flags[pp], 1u) == 0u) return;
+        p = pp;
+    }
+}
+
 cudaError_t launch_lbvh_refit(const gray_params &p, cudaStream_t s) {
     const int n = p.gaussians.count;
     if (n <= 0) return cudaSuccess;
     const gray_scene &sc = p.scene;
+    cudaError_t e;
     if (n > 1) {
-        cudaError_t e = cudaMemsetAsync(sc.refit_flags, 0, sizeof(uint32_t) * (size_t)(n - 1), s);
+        e = cudaMemsetAsync(sc.refit_flags, 0, sizeof(uint32_t) * (size_t)(n - 1), s);
         if (e != cudaSuccess) return e;
     }
-    refit_kernel<<<blocks_for(n), kThreads, 0, s>>>(n, reinterpret_cast<const float4 *>(sc.aabb), sc.order,
-                                                   sc.leaf_parent, sc.int_parent, sc.nodes, sc.refit_flags,
-                                                   sc.root_box);
+    const unsigned int blocks = blocks_for(n);
+    if (sc.sort_tmp && n > 1) {
+        // queue in the sort scratch (free outside a build's sort): count, then <= blocks - 1 nodes
+        uint32_t *queue = sc.sort_tmp;
+        if ((e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
+        refit_local_kernel<<<blocks, kThreads, 0, s>>>(n, reinterpret_cast<const float4 *>(sc.aabb), sc.order,
+                                                       sc.leaf_parent, sc.int_parent, sc.nodes, sc.refit_flags, queue,
+                                                       sc.root_box);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        refit_top_kernel<<<blocks_for(blocks), kThreads, 0, s>>>(sc.int_parent, sc.nodes, sc.refit_flags, queue,
+                                                                 sc.root_box);
+        return cudaGetLastError();
+    }
+    refit_kernel<<<blocks, kThreads, 0, s>>>(n, reinterpret_cast<const float4 *>(sc.aabb), sc.order, sc.leaf_parent,
+                                             sc.int_parent, sc.nodes, sc.refit_flags, sc.root_box);
     return cudaGetLastError();
 }
 
