@@ -362,7 +362,9 @@ __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const floa
     int lo = k, hi = k;
     uint32_t link = gid | GRAY_LEAF_BIT;
     for (int guard = 0; guard < 128; guard++) {
+        // the parent's links and its own parent, loaded together (one round trip per level)
         const float4 q3 = __ldcg(reinterpret_cast<const float4 *>(nodes) + 4 * (size_t)p + 3);
+        const int pnext = int_parent[p];
         const int slot = __float_as_uint(q3.x) == link ? 0 : 1;
         const int leaves = (int)__float_as_uint(q3.z);
         const int plo = slot == 0 ? lo : hi - leaves + 1, phi = slot == 0 ? lo + leaves - 1 : hi;
@@ -388,7 +390,7 @@ __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const floa
         lo = plo;
         hi = phi;
         link = (uint32_t)p;
-        p = int_parent[p];
+        p = pnext;
         if (p < 0) {
             write_root_box(root_box, box);
             return;

@@ -1771,11 +1771,12 @@ __device__ __forceinline__ void replay_hit(const BwdArgs &a, const BwdPixel &px,
     T = T / om;
 }
 
-// One thread per pixel walks its composited hits back to front (16x8-pixel blocks, so a warp holds
-// two rows of 16 neighbouring pixels).
+// One thread per pixel walks its composited hits back to front (16x8-pixel blocks of four 8x4-pixel
+// warps: neighbouring pixels composite the same Gaussians, which the lanes combine cheaply).
 __global__ void __launch_bounds__(128) trace_backward_kernel(const BwdArgs a) {
-    const int px = blockIdx.x * 16 + (threadIdx.x & 15);
-    const int py = blockIdx.y * 8 + (threadIdx.x >> 4);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int px = blockIdx.x * 16 + (w & 1) * 8 + (l & 7);
+    const int py = blockIdx.y * 8 + (w >> 1) * 4 + (l >> 3);
     if (px >= (int)a.render_w || py >= (int)a.render_h) return;
     const uint32_t pixel = (uint32_t)py * a.alloc_w + (uint32_t)px;
     HitCursor cur;

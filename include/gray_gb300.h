@@ -143,7 +143,9 @@ typedef struct gray_scene {
     uint32_t *order;      /* [N] sorted leaf position -> gaussian id */
     uint32_t *codes;      /* [N] Morton codes in sorted order */
     uint32_t *refit_flags;/* [max(N-1,1)] */
-    uint32_t *sort_tmp;   /* [sort_tmp_words] */
+    uint32_t *sort_tmp;   /* [sort_tmp_words] radix-sort scratch of a rebuild; a refit queues the
+                             upper tree's first nodes in it (may be NULL for gray_update_bvh: the
+                             refit then climbs the whole tree with global counters, slower) */
     float *root_box;      /* [8] */
     uint32_t *bounds;     /* [8] order-preserving encoded scene bounds (scratch) */
     float *bwd_rec;       /* [N,24] per-Gaussian backward record, written at the start of each

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 import torch
 
-from gray_gb300 import synthetic
+from gray_gb300 import _lib, synthetic
 from tests import gpu_util as G
 
 pytestmark = pytest.mark.gpu
@@ -124,6 +124,16 @@ def test_snapshot_and_bvh_bit_exact(oracle):
                                         sc.opacity[:, 0])
     tree.refit(aabb2)
     assert np.array_equal(ws.aabb.cpu().numpy(), aabb2)
+    assert np.array_equal(ws.nodes.cpu().numpy(), tree.nodes)
+    assert np.array_equal(ws.root_box.cpu().numpy(), tree.root_box)
+    # a refit without the sort scratch (every level through global counters) gives the same boxes
+    with torch.no_grad():
+        ws.nodes[:, :12].fill_(-1.0)
+        ws.root_box.fill_(-1.0)
+    params = rt._build_params()
+    params.scene.sort_tmp = None
+    _lib.call("gray_update_bvh", params, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
     assert np.array_equal(ws.nodes.cpu().numpy(), tree.nodes)
     assert np.array_equal(ws.root_box.cpu().numpy(), tree.root_box)
 
