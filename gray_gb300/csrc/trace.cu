@@ -1200,9 +1200,7 @@ __device__ __forceinline__ void ellipsoid_leaf(const FwdArgs &a, uint32_t gid, f
 
 constexpr int kEllTileX = 16, kEllTileY = 8;
 
-__global__ void __launch_bounds__(kEllTileX * kEllTileY) ellipsoid_kernel(const FwdArgs a) {
-    if (!*a.render_ellipsoids) return;
-    const int px = blockIdx.x * kEllTileX + threadIdx.x, py = blockIdx.y * kEllTileY + threadIdx.y;
+__device__ __forceinline__ void ellipsoid_pixel(const FwdArgs &a, int px, int py) {
     if (px >= (int)a.render_w || py >= (int)a.render_h) return;
     const uint32_t pixel = (uint32_t)py * a.alloc_w + (uint32_t)px;
     if (!a.display && *a.grads_enabled) raise_status(a.status, GRAY_STATUS_BAD_MODE);
@@ -1288,6 +1286,14 @@ __global__ void __launch_bounds__(kEllTileX * kEllTileY) ellipsoid_kernel(const 
     a.out_rgb[3 * pixel + 1] = r1;
     a.out_rgb[3 * pixel + 2] = r2;
     a.out_depth[pixel] = depth;
+}
+
+// Grid-stride over 16x8-pixel tiles (a few blocks per SM): the launch made on every forward costs
+// little when the view is off.
+__global__ void __launch_bounds__(kEllTileX * kEllTileY) ellipsoid_kernel(const FwdArgs a, int tiles_x, int ntiles) {
+    if (!*a.render_ellipsoids) return;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
+        ellipsoid_pixel(a, (t % tiles_x) * kEllTileX + threadIdx.x, (t / tiles_x) * kEllTileY + threadIdx.y);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1468,8 +1474,15 @@ static FwdArgs forward_args(const gray_params &p, bool display) {
 
 cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s) {
     const FwdArgs a = forward_args(p, display);
-    dim3 grid((p.render_width + kEllTileX - 1) / kEllTileX, (p.render_height + kEllTileY - 1) / kEllTileY);
-    ellipsoid_kernel<<<grid, dim3(kEllTileX, kEllTileY), 0, s>>>(a);
+    const int tiles_x = (int)((p.render_width + kEllTileX - 1) / kEllTileX);
+    const int ntiles = tiles_x * (int)((p.render_height + kEllTileY - 1) / kEllTileY);
+    if (ntiles <= 0) return cudaSuccess;
+    int dev = 0, sms = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const int grid = ntiles < 8 * sms ? ntiles : 8 * sms;
+    ellipsoid_kernel<<<grid, dim3(kEllTileX, kEllTileY), 0, s>>>(a, tiles_x, ntiles);
     return cudaGetLastError();
 }
 
