@@ -245,6 +245,54 @@ __device__ __forceinline__ void add_log_transmittance(long long &s, float alpha)
 }
 __device__ __forceinline__ float full_transmittance(long long s) { return gexp(__ll2float_rn(s) * 0x1.0p-40f); }
 
+// Object-space origin lo = M (o - mu) of a snapshot (rows g0..g2 = (M | mu)), as local_ray computes it.
+__device__ __forceinline__ f3 local_origin(const float4 g0, const float4 g1, const float4 g2, f3 ro) {
+    const f3 rel = mk3(ro.x - g0.w, ro.y - g1.w, ro.z - g2.w);
+    return mk3(fdot3(g0, rel), fdot3(g1, rel), fdot3(g2, rel));
+}
+
+// local_ray for rows whose w column already holds the object-space origin lo (rays that share one
+// origin: lo is computed once per Gaussian with local_origin, the same arithmetic).
+__device__ __forceinline__ void local_ray_lo(const float4 m0, const float4 m1, const float4 m2, f3 rd, LocalHit &h) {
+    h.lo = mk3(m0.w, m1.w, m2.w);
+    h.ld = mk3(fdot3(m0, rd), fdot3(m1, rd), fdot3(m2, rd));
+    h.b = fdot3(h.lo, h.ld);
+}
+
+// intersect() for rows (M | lo) from local_origin: the same arithmetic, so the same answer.
+__device__ __forceinline__ bool intersect_lo(const float4 m0, const float4 m1, const float4 m2, float o, float sf,
+                                             f3 rd, float alpha_threshold, float exp_power, float znear, float zfar,
+                                             float &dist, float &alpha) {
+    if (o <= alpha_threshold) return false;
+    LocalHit h;
+    local_ray_lo(m0, m1, m2, rd, h);
+    if (h.b > 0.0f) return false;
+    closest_point(h);
+    float sq = fdot3(h.u, h.u);
+    if (sq > 1.0f) return false;
+    dist = h.t;
+    if (!(dist >= znear && dist <= zfar)) {
+        if (!unit_box_overlap(h, znear, zfar)) return false;
+    }
+    f3 x = mk3(h.u.x * sf, h.u.y * sf, h.u.z * sf);
+    float gv = eval_gaussian(fdot3(x, x), exp_power);
+    alpha = maxalpha_mul(gv, o);
+    return true;
+}
+
+// The hit decision of intersect_lo() alone.
+__device__ __forceinline__ bool intersect_hits_lo(const float4 m0, const float4 m1, const float4 m2, float o, f3 rd,
+                                                  float alpha_threshold, float znear, float zfar) {
+    if (o <= alpha_threshold) return false;
+    LocalHit h;
+    local_ray_lo(m0, m1, m2, rd, h);
+    if (h.b > 0.0f) return false;
+    closest_point(h);
+    if (fdot3(h.u, h.u) > 1.0f) return false;
+    if (!(h.t >= znear && h.t <= zfar)) return unit_box_overlap(h, znear, zfar);
+    return true;
+}
+
 // The hit decision of intersect() alone (same arithmetic, so the same answer), without the
 // Gaussian response.
 __device__ __forceinline__ bool intersect_hits(const float4 g0, const float4 g1, const float4 g2, float o, f3 ro,

@@ -153,13 +153,18 @@ struct RayResult {
 
 // Intersection program + all-hit sums + selection for one (ray, Gaussian) pair whose snapshot rows,
 // live values and colour the caller has fetched.
-template <int KB>
+// LO: the rows' w column holds the object-space origin (local_origin) instead of the mean.
+template <int KB, bool LO = false>
 __device__ __forceinline__ void on_leaf_data(uint32_t gid, const float4 g0, const float4 g1, const float4 g2,
                                              const float2 lv, int cf0, int cf1, int cf2, bool first, f3 ro, f3 rd,
                                              const TraceKnobs &k, LaneState &st,
                                              unsigned long long (*kbuf)[kFwdThreads]) {
     float dist, alpha;
-    if (!intersect(g0, g1, g2, lv.x, lv.y, ro, rd, k.athr, k.pw, k.znear, k.zfar, dist, alpha)) return;
+    if constexpr (LO) {
+        if (!intersect_lo(g0, g1, g2, lv.x, lv.y, rd, k.athr, k.pw, k.znear, k.zfar, dist, alpha)) return;
+    } else {
+        if (!intersect(g0, g1, g2, lv.x, lv.y, ro, rd, k.athr, k.pw, k.znear, k.zfar, dist, alpha)) return;
+    }
     const uint16_t a16 = f2h_bits(alpha), d16 = f2h_bits(dist);
     if (first) {
         add_log_transmittance(st.lfx, alpha);
@@ -209,7 +214,7 @@ __device__ __forceinline__ void on_leaf(const TraceScene &sc, uint32_t gid, bool
 // Per-warp shared-memory copy of the queued leaves' records, filled once per flush by the lanes
 // (one candidate each, all loads in flight together) and read by every lane afterwards.
 struct CandCache {
-    float4 g[kCand][3];  // snapshot rows (M | mu)
+    float4 g[kCand][3];  // snapshot rows with the packet's object-space origin: (M | M (o - mu))
     int4 c[kCand];       // colour in 2^-24 fixed point (x, y, z), live opacity bits (w)
     float sf[kCand];     // live scaling factor
 };
@@ -307,12 +312,15 @@ __device__ __forceinline__ bool frustum_ellipsoid(const Frustum &fr, const float
 // Processes the packet's queued leaves (cand[0, nc), at most kCand = 32; every lane of the warp calls
 // this together).  (1) Lane j takes candidate j: it tests the candidate's ellipsoid against the
 // packet frustum and fetches its snapshot rows, live values and colour; the survivors are
-// compacted into the warp's shared-memory cache.  (2) Every lane runs the hit test of its own ray
+// compacted into the warp's shared-memory cache, each with its object-space ray origin (the
+// packet's rays share the origin, so it is computed once per candidate, not once per lane).  (2) Every lane runs the hit test of its own ray
 // against every cached candidate and keeps a 32-bit mask of its hits.  (3) The lanes walk their
 // masks together, one hit per lane per step, through the intersection program and the selection.
 // The order in which a lane sees its hits does not matter: the all-hit sums are order-independent
-// and the selection is by key.
-template <int KB>
+// and the selection is by key.  LO: the cache keeps each candidate's object-space ray origin in
+// place of its mean (computed once by the fetching lane; saves 12 instructions per hit test but
+// needs registers, so the register-capped kernels keep the mean and recompute per lane).
+template <int KB, bool LO>
 __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool want,
                                                  bool first, LaneState &st, unsigned long long (*kbuf)[kFwdThreads],
                                                  const Frustum &fr, uint32_t *cand, CandCache &cc, int nc) {
@@ -333,6 +341,12 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
         cv = make_int4(colour_fixed(cp[0]), colour_fixed(cp[1]), colour_fixed(cp[2]), __float_as_int(lv.x));
         sfv = lv.y;
         keep = sc.l2w ? frustum_ellipsoid(fr, sc.l2w + 3 * (size_t)gid) : true;
+        if constexpr (LO) {
+            const f3 lo = local_origin(g0, g1, g2, ro);
+            g0.w = lo.x;
+            g1.w = lo.y;
+            g2.w = lo.z;
+        }
     }
     const uint32_t bal = __ballot_sync(kFull, keep);
     __syncwarp();  // every read of cand[] precedes the compacting writes
@@ -350,9 +364,14 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
     uint32_t mask = 0u;
     if (want) {
         for (int j = 0; j < nc; j++) {
-            if (intersect_hits(cc.g[j][0], cc.g[j][1], cc.g[j][2], __int_as_float(cc.c[j].w), ro, rd, k.athr,
-                               k.znear, k.zfar))
+            if constexpr (LO) {
+                if (intersect_hits_lo(cc.g[j][0], cc.g[j][1], cc.g[j][2], __int_as_float(cc.c[j].w), rd, k.athr,
+                                      k.znear, k.zfar))
+                    mask |= 1u << j;
+            } else if (intersect_hits(cc.g[j][0], cc.g[j][1], cc.g[j][2], __int_as_float(cc.c[j].w), ro, rd, k.athr,
+                                      k.znear, k.zfar)) {
                 mask |= 1u << j;
+            }
         }
     }
     while (__any_sync(kFull, mask != 0u)) {
@@ -360,8 +379,9 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
             const int j = __ffs(mask) - 1;
             mask &= mask - 1u;
             const int4 c = cc.c[j];
-            on_leaf_data<KB>(cand[j], cc.g[j][0], cc.g[j][1], cc.g[j][2], make_float2(__int_as_float(c.w), cc.sf[j]),
-                             c.x, c.y, c.z, first, ro, rd, k, st, kbuf);
+            on_leaf_data<KB, LO>(cand[j], cc.g[j][0], cc.g[j][1], cc.g[j][2],
+                                   make_float2(__int_as_float(c.w), cc.sf[j]), c.x, c.y, c.z, first, ro, rd, k, st,
+                                   kbuf);
         }
     }
     __syncwarp();
@@ -375,7 +395,7 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
 // of at the root: the frontier goes onto the stack with its first entry on top, and a frontier leaf
 // is queued when it is popped.  Returns false if the shared stack overflowed (the caller then
 // repeats the traversal per ray).
-template <int KB>
+template <int KB, bool LO>
 __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool want,
                                                  bool first, LaneState &st, unsigned long long (*kbuf)[kFwdThreads],
                                                  const Frustum &fr, uint32_t *stk, uint32_t *cand,
@@ -469,7 +489,7 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
         while (nc >= kCand || (draining && nc > 0)) {
             // process the first kCand queued leaves, then move the rest to the front
             const int take = nc < kCand ? nc : kCand;
-            flush_candidates<KB>(sc, k, ro, rd, want, first, st, kbuf, fr, cand, cc, take);
+            flush_candidates<KB, LO>(sc, k, ro, rd, want, first, st, kbuf, fr, cand, cc, take);
             const int rest = nc - take;
             const uint32_t r0 = lane < rest ? cand[kCand + lane] : 0u;
             const uint32_t r1 = lane + 32 < rest ? cand[kCand + 32 + lane] : 0u;
@@ -488,7 +508,7 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
 // Trace the warp's 32 rays (one per lane; `alive` lanes only) through the scene: traversal,
 // selection, compositing (cuda/forward_pass.cu:6-151 minus the write-out).  Every lane of the
 // warp must call this together.
-template <int KB>
+template <int KB, bool LO>
 __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool alive,
                                           bool grads, const HitSink &hs, int32_t *status,
                                           unsigned long long (*kbuf)[kFwdThreads], RayResult &res,
@@ -521,7 +541,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
         // ---------------- traversal ----------------
         bool per_ray = fr == nullptr;
         if (!per_ray &&
-            !traverse_frustum<KB>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, *wcc, front, status)) {
+            !traverse_frustum<KB, LO>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, *wcc, front, status)) {
             // the frustum traversal gave up (stack overflow): discard what it gathered, trace per ray
             st.kcount = 0;
             st.ncand = 0;
@@ -764,7 +784,7 @@ struct FwdShared {
 };
 
 // One block's pixel tile (bx, by): 2x2 packets of tile_w x tile_h pixels, one per warp.
-template <int KB>
+template <int KB, bool LO>
 __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, FwdShared<KB> &sh) {
     unsigned long long(*kbuf)[kFwdThreads] = sh.kbuf;
     Frustum *sfr = sh.sfr;
@@ -788,6 +808,11 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
     // ---- ray generation (cuda/shaders.cu:76-88) ----
     f3 ro = mk3(0.0f, 0.0f, 0.0f), rd = mk3(0.0f, 0.0f, 0.0f);
     bool alive = false;
+    // LO: every lane holds the camera origin, inactive ones too (a packet's candidates get their
+    // object-space origin from whichever lane fetches them)
+    if constexpr (LO) {
+        if (!*a.rays_from_python) ro = mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]);
+    }
     if (inside) {
         if (*a.rays_from_python) {
             ro = mk3(a.ray_o[3 * pixel], a.ray_o[3 * pixel + 1], a.ray_o[3 * pixel + 2]);
@@ -831,7 +856,7 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
         __syncwarp();
     }
     RayResult r;
-    trace_ray<KB>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sh.sstk[warp],
+    trace_ray<KB, LO>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sh.sstk[warp],
                   sh.scand[warp], &sh.scc[warp], sh.front);
 
     if (!inside) return;
@@ -877,7 +902,7 @@ template <int KB, int MINB>
 __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const FwdArgs a) {
     __shared__ FwdShared<KB> sh;
     if (*a.render_ellipsoids) return;  // the ellipsoid view (ellipsoid_kernel) renders this frame
-    forward_tile<KB>(a, blockIdx.x, blockIdx.y, sh);
+    forward_tile<KB, (MINB < 6)>(a, blockIdx.x, blockIdx.y, sh);
 }
 
 // Persistent launch: the blocks take tiles from the schedule's order, densest first, until none is
@@ -894,7 +919,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_sched_kernel(
         const uint32_t t = s_next;
         if (t >= (uint32_t)a.ntiles) break;
         const uint32_t tile = a.schedule[kSchedHeader + a.ntiles + t];
-        forward_tile<KB>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x), sh);
+        forward_tile<KB, (MINB < 6)>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x), sh);
     }
 }
 
@@ -1407,7 +1432,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
             front = frontier + (size_t)(vw.group_offset + (ty / 2) * ((tiles_x + 1) / 2) + tx / 2) * kFrontierWords;
         }
         RayResult r;
-        trace_ray<KB>(sc, k, ro, rd, inside, false, hs, status, kbuf, r, &sfr[warp], sstk[warp], scand[warp],
+        trace_ray<KB, (MINB < 6)>(sc, k, ro, rd, inside, false, hs, status, kbuf, r, &sfr[warp], sstk[warp], scand[warp],
                       &scc[warp], front);
         if (!inside) continue;
         float r0, r1, r2;
