@@ -247,7 +247,13 @@ struct Frustum {
 // coordinate magnitude of the root box, the tests' sums have magnitude at most |n|_1 (4M + 2|o|_1)
 // and a few roundings of 2^-24 each; the thresholds leave 1e-5 of that (about 170 roundings).
 // Boxes with an infinite or NaN coordinate (beyond M) give an infinite or NaN sum and always pass.
-__device__ __forceinline__ void make_frustum(Frustum &fr, f3 o, const f3 d[4], const float *root_box) {
+__device__ __forceinline__ float3 camera_ray3(const float *w, float fov, int px, int py, uint32_t width,
+                                              uint32_t height);
+
+// Plane e of the frustum (e < 4: the side through corner rays e and e+1; e = 4: the near plane
+// orthogonal to the corners' sum).
+__device__ __forceinline__ void frustum_plane(int e, f3 o, const f3 d[4], const float *root_box, float4 &pn,
+                                              float4 &pa) {
     const f3 c = mk3(d[0].x + d[1].x + d[2].x + d[3].x, d[0].y + d[1].y + d[2].y + d[3].y,
                      d[0].z + d[1].z + d[2].z + d[3].z);
     float m = 0.0f;
@@ -257,21 +263,34 @@ __device__ __forceinline__ void make_frustum(Frustum &fr, f3 o, const f3 d[4], c
         if (i != 3 && i != 7 && v <= 0x1.fffffep127f) m = fmaxf(m, v);
     }
     const float o1 = fabsf(o.x) + fabsf(o.y) + fabsf(o.z);
-#pragma unroll
-    for (int e = 0; e < 5; e++) {
-        f3 nn = c;
-        if (e < 4) {
-            const f3 a = d[e], b = d[(e + 1) & 3];
-            nn = mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-            if (dot3(nn, c) < 0.0f) nn = mk3(-nn.x, -nn.y, -nn.z);
-        }
-        const float n1 = fabsf(nn.x) + fabsf(nn.y) + fabsf(nn.z);
-        const float no = fdot3(nn, o);
-        const float mbox = 1e-5f * n1 * (4.0f * m + 2.0f * o1) + 1e-30f;
-        const float mell = 1e-5f * n1 * (3.0f * m + o1) + 1e-30f;
-        fr.pn[e] = make_float4(nn.x, nn.y, nn.z, 2.0f * no - mbox);
-        fr.pa[e] = make_float4(fabsf(nn.x), fabsf(nn.y), fabsf(nn.z), no - mell);
+    f3 nn = c;
+    if (e < 4) {
+        const f3 a = d[e], b = d[(e + 1) & 3];
+        nn = mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+        if (dot3(nn, c) < 0.0f) nn = mk3(-nn.x, -nn.y, -nn.z);
     }
+    const float n1 = fabsf(nn.x) + fabsf(nn.y) + fabsf(nn.z);
+    const float no = fdot3(nn, o);
+    const float mbox = 1e-5f * n1 * (4.0f * m + 2.0f * o1) + 1e-30f;
+    const float mell = 1e-5f * n1 * (3.0f * m + o1) + 1e-30f;
+    pn = make_float4(nn.x, nn.y, nn.z, 2.0f * no - mbox);
+    pa = make_float4(fabsf(nn.x), fabsf(nn.y), fabsf(nn.z), no - mell);
+}
+
+// The frustum built by a whole warp (every lane calls this): lanes 0-3 trace one corner ray each,
+// lanes 0-4 write one plane each.
+__device__ __forceinline__ void make_frustum_warp(Frustum &fr, f3 o, const float *w2c, float fov, int x0, int y0,
+                                                  int x1, int y1, uint32_t width, uint32_t height,
+                                                  const float *root_box) {
+    const int lane = threadIdx.x & 31;
+    float3 dl = make_float3(0.0f, 0.0f, 0.0f);
+    if (lane < 4) dl = camera_ray3(w2c, fov, (lane == 1 || lane == 2) ? x1 : x0, lane >= 2 ? y1 : y0, width, height);
+    f3 d[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++)
+        d[e] = mk3(__shfl_sync(0xffffffffu, dl.x, e), __shfl_sync(0xffffffffu, dl.y, e), __shfl_sync(0xffffffffu, dl.z, e));
+    if (lane < 5) frustum_plane(lane, o, d, root_box, fr.pn[lane], fr.pa[lane]);
+    __syncwarp();
 }
 
 // Conservative box-frustum test: false only when the box lies entirely outside one plane by more
@@ -772,6 +791,12 @@ __device__ __forceinline__ f3 camera_ray(const float *w, float fov, int px, int 
     return mk3(v.x * inv, v.y * inv, v.z * inv);
 }
 
+__device__ __forceinline__ float3 camera_ray3(const float *w, float fov, int px, int py, uint32_t width,
+                                              uint32_t height) {
+    const f3 r = camera_ray(w, fov, px, py, width, height, 0.0f, 0.0f);
+    return make_float3(r.x, r.y, r.z);
+}
+
 // Shared memory of a forward block.
 template <int KB>
 struct FwdShared {
@@ -845,15 +870,8 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
     if (frustum) {
         const int x0 = px - lane % a.tile_w, y0 = py - lane / a.tile_w;
         const int x1 = x0 + a.tile_w - 1, y1 = y0 + a.tile_h - 1;
-        if (lane == 0) {
-            const f3 o = mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]);
-            const f3 d[4] = {camera_ray(a.w2c, *a.fov, x0, y0, a.render_w, a.render_h, 0.0f, 0.0f),
-                             camera_ray(a.w2c, *a.fov, x1, y0, a.render_w, a.render_h, 0.0f, 0.0f),
-                             camera_ray(a.w2c, *a.fov, x1, y1, a.render_w, a.render_h, 0.0f, 0.0f),
-                             camera_ray(a.w2c, *a.fov, x0, y1, a.render_w, a.render_h, 0.0f, 0.0f)};
-            make_frustum(sfr[warp], o, d, a.root_box);
-        }
-        __syncwarp();
+        make_frustum_warp(sfr[warp], mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]), a.w2c, *a.fov, x0, y0, x1,
+                          y1, a.render_w, a.render_h, a.root_box);
     }
     RayResult r;
     trace_ray<KB, LO>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sh.sstk[warp],
@@ -1103,15 +1121,8 @@ __global__ void __launch_bounds__(32) tile_cost_kernel(const FwdArgs a, int bw, 
     if (!*a.rays_from_python && !*a.jitter && !*a.render_ellipsoids && n > 1) {
         const int x0 = (tile % a.tiles_x) * bw, y0 = (tile / a.tiles_x) * bh;
         const int x1 = min(x0 + bw, (int)a.render_w) - 1, y1 = min(y0 + bh, (int)a.render_h) - 1;
-        if (lane == 0) {
-            const f3 o = mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]);
-            const f3 d[4] = {camera_ray(a.w2c, *a.fov, x0, y0, a.render_w, a.render_h, 0.0f, 0.0f),
-                             camera_ray(a.w2c, *a.fov, x1, y0, a.render_w, a.render_h, 0.0f, 0.0f),
-                             camera_ray(a.w2c, *a.fov, x1, y1, a.render_w, a.render_h, 0.0f, 0.0f),
-                             camera_ray(a.w2c, *a.fov, x0, y1, a.render_w, a.render_h, 0.0f, 0.0f)};
-            make_frustum(fs.fr, o, d, a.root_box);
-        }
-        __syncwarp();
+        make_frustum_warp(fs.fr, mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]), a.w2c, *a.fov, x0, y0, x1, y1,
+                          a.render_w, a.render_h, a.root_box);
         est = frontier_walk(a.nodes, n, a.frontier_cut > 0 ? a.frontier_cut : (uint32_t)kCostCut, fs, out);
     } else if (out && lane == 0) {
         out[0] = kFrontierNone;
@@ -1356,15 +1367,8 @@ __global__ void __launch_bounds__(32) batch_frontier_kernel(const gray_batch_sce
         return;
     }
     const int x1 = min(x0 + 2 * tile_w, (int)vw.width) - 1, y1 = min(y0 + 2 * tile_h, (int)vw.height) - 1;
-    if (lane == 0) {
-        const f3 o = mk3(vw.origin[0], vw.origin[1], vw.origin[2]);
-        const f3 d[4] = {camera_ray(vw.w2c, vw.fov_y, x0, y0, vw.width, vw.height, 0.0f, 0.0f),
-                         camera_ray(vw.w2c, vw.fov_y, x1, y0, vw.width, vw.height, 0.0f, 0.0f),
-                         camera_ray(vw.w2c, vw.fov_y, x1, y1, vw.width, vw.height, 0.0f, 0.0f),
-                         camera_ray(vw.w2c, vw.fov_y, x0, y1, vw.width, vw.height, 0.0f, 0.0f)};
-        make_frustum(fs.fr, o, d, bs.root_box);
-    }
-    __syncwarp();
+    make_frustum_warp(fs.fr, mk3(vw.origin[0], vw.origin[1], vw.origin[2]), vw.w2c, vw.fov_y, x0, y0, x1, y1, vw.width,
+                      vw.height, bs.root_box);
     frontier_walk(reinterpret_cast<const float4 *>(bs.nodes), bs.n, cut, fs, out);
 }
 
@@ -1416,16 +1420,11 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
         f3 ro = mk3(vw.origin[0], vw.origin[1], vw.origin[2]);
         f3 rd = mk3(0.0f, 0.0f, 0.0f);
         if (inside) rd = camera_ray(vw.w2c, vw.fov_y, px, py, vw.width, vw.height, 0.0f, 0.0f);
-        if (lane == 0) {
+        {
             const int x0 = (int)((local % tiles_x) * tile_w), y0 = (int)((local / tiles_x) * tile_h);
-            const int x1 = x0 + tile_w - 1, y1 = y0 + tile_h - 1;
-            const f3 d[4] = {camera_ray(vw.w2c, vw.fov_y, x0, y0, vw.width, vw.height, 0.0f, 0.0f),
-                             camera_ray(vw.w2c, vw.fov_y, x1, y0, vw.width, vw.height, 0.0f, 0.0f),
-                             camera_ray(vw.w2c, vw.fov_y, x1, y1, vw.width, vw.height, 0.0f, 0.0f),
-                             camera_ray(vw.w2c, vw.fov_y, x0, y1, vw.width, vw.height, 0.0f, 0.0f)};
-            make_frustum(sfr[warp], ro, d, s_sc[warp].root_box);
+            make_frustum_warp(sfr[warp], ro, vw.w2c, vw.fov_y, x0, y0, x0 + tile_w - 1, y0 + tile_h - 1, vw.width,
+                              vw.height, s_sc[warp].root_box);
         }
-        __syncwarp();
         const uint32_t *front = nullptr;
         if (frontier) {
             const uint32_t tx = local % tiles_x, ty = local / tiles_x;
