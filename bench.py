@@ -342,7 +342,7 @@ def gpu_arm(a, rank, world, local_rank):
         "trace_backward": 120.0 * A + 72.0 * R,
         "forward_prep": 228.0 * n,
         "fold_sh_backward": 460.0 * n,
-        "adam": 1984.0 * n,
+        "adam": (59 * 32.0 + 12.0) * n,  # 59 Adam floats x (p, m, v, g) read + written; channel grads zeroed
         "snapshot": (44.0 + 48 + 48 + 32) * n,
         "refit": 44.0 * n + 24.0 * (2 * n - 1),
     }
