@@ -81,3 +81,27 @@ def test_ctypes_structs_match_c_layout(tmp_path):
         assert int(c[f"{cname} size"]) == ctypes.sizeof(cls), cname
         for f, _ in cls._fields_:
             assert int(c[f"{cname}.{f}"]) == getattr(cls, f).offset, f"{cname}.{f}"
+
+
+def _ceil(a, b):
+    return -(-a // b)
+
+
+def test_frontier_and_batch_sizes(gray_lib):
+    """Workspace sizing without a GPU: the frontier record length matches the header, a batch view's
+    packet groups are its 2x2 packets, and a framebuffer's schedule holds the estimates, the order
+    and a frontier per block tile for both packet shapes (8x16- and 16x8-pixel tiles)."""
+    from gray_gb300 import batch
+
+    L = batch._bind()
+    m = re.search(r"#define GRAY_FRONTIER_WORDS (\d+)", open(HEADER).read())
+    words = int(L.gray_frontier_words())
+    assert m and words == int(m.group(1))
+    header = 64
+    for w, h in ((1, 1), (7, 5), (640, 480), (1600, 1040), (1920, 1080), (3840, 2160), (1001, 333)):
+        for variant, (tw, th) in ((7, (4, 8)), (3, (8, 4))):
+            packets = _ceil(w, tw) * _ceil(h, th)
+            assert L.gray_batch_packets(w, h, variant) == packets
+            assert L.gray_batch_groups(w, h, variant) == _ceil(_ceil(w, tw), 2) * _ceil(_ceil(h, th), 2)
+            tiles = _ceil(w, 2 * tw) * _ceil(h, 2 * th)  # the forward's block tiles (2x2 packets)
+            assert gray_lib.gray_schedule_words(w, h) >= header + tiles * (2 + words), (w, h, variant)
