@@ -1,20 +1,27 @@
 // trace.cu -- forward and backward ray tracing of the Gaussians on the LBVH.
 //
 // Forward (replaces the OptiX launch of cuda/shaders.cu:69-106 with cuda/forward_pass.cu):
-//   A warp traces an 8x4 pixel tile as one packet: the traversal stack is warp-uniform (held
-//   across the lanes' registers), every lane tests its own ray against both child boxes of the
-//   popped node and the warp descends where any lane hits.  Leaves run the intersection
-//   program of cuda/shaders.cu:10-67 per lane.  The first traversal accumulates, over ALL hits,
-//   the full transmittance and (in 64-bit fixed point) the alpha-weighted colour sums the
-//   reference uses for its truncated-tail estimate, and every traversal keeps the KB nearest
-//   hits above a resume key in a per-lane shared-memory buffer of 64-bit keys
-//   (fp16 distance | gaussian id | fp16 alpha).  The buffer is consumed by a state machine that
-//   reproduces the reference's 32-slot multi-pass selection exactly (pass boundaries, the
-//   strict `distance > tmin` drop of equal distances, the 99-pass cap, zfar, t_threshold).
-//   Composited ids are appended to the backward hit list in warp-aggregated segments.
+//   A block renders an 8x16-pixel tile, each warp a 4x8 (or 8x4) pixel packet of camera rays that
+//   share one origin.  A per-tile kernel first walks the top of the BVH with the tile's frustum and
+//   records the tile's frontier (the nodes of at most 64 leaves it reaches, sorted front to back);
+//   every packet traversal starts there.  The packet traverses as a frustum: each step pops up to
+//   32 nodes (one per lane) from a per-warp shared-memory stack, tests both child boxes against the
+//   frustum, pushes the nearer child last and queues leaves; queued leaves are culled by an exact
+//   ellipsoid-frustum test, cached in shared memory, hit-tested by every lane against its own ray,
+//   and the lanes then walk their hit masks through the intersection program of
+//   cuda/shaders.cu:10-67.  The first traversal accumulates, over ALL hits, the full transmittance
+//   (an order-independent fixed-point sum of log(1 - alpha)) and the alpha-weighted colour sums of
+//   the reference's truncated-tail estimate, and every traversal keeps the KB nearest hits above a
+//   resume key in a per-lane shared-memory buffer of 64-bit keys (fp16 distance | gaussian id |
+//   fp16 alpha).  The buffer is consumed by a state machine that reproduces the reference's
+//   32-slot multi-pass selection exactly (pass boundaries, the strict `distance > tmin` drop of
+//   equal distances, the 99-pass cap, zfar, t_threshold).  Composited ids are appended to the
+//   backward hit list in warp-aggregated segments.  Rays from Python, jittered rays and packets
+//   whose traversal overflows the shared stack take a per-ray slab traversal instead.
 // Backward (cuda/backward_pass.cu:2-142): one thread per pixel walks its segments back to front,
 //   recomputes alpha in fp32 and reduces the 16 per-hit gradient values into the per-Gaussian
-//   accumulator with four 16-byte vector reductions.
+//   accumulator: lanes holding the same Gaussian combine in a tree, and the lowest issues four
+//   16-byte vector reductions.
 #include "gray_device.cuh"
 #include "gray_internal.h"
 
