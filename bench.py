@@ -363,6 +363,7 @@ def gpu_arm(a, rank, world, local_rank):
                 "hits_per_ray": round(H / R, 2), "composited_per_ray": round(A / R, 2)}
 
     batched = None if a.no_extras else batched_form(a, rt.cuda_module)
+    differentiation = None if a.no_extras else differentiation_form(a, rt.cuda_module, cam, target_dev)
     served = None if (a.no_extras or a.no_served) else served_form(a, rank)
 
     cpu = None
@@ -379,7 +380,7 @@ def gpu_arm(a, rank, world, local_rank):
                     "upload": "pinned host -> device on a copy stream, overlapped with the previous step",
                     "serial_value": round(whole_job_rate(a.steps, ms_e2e_serial, world), 3)},
             "gpu_launches": launches, "roofline": roofline, "clocks": clk, "cpu_baseline": cpu,
-            "batched": batched, "served": served}
+            "batched": batched, "differentiation": differentiation, "served": served}
     return line
 
 
@@ -427,6 +428,41 @@ def batched_form(a, tracer):
             "plain_rays_per_s": round(rays / ms_plain * 1000.0, 1),
             "batched_rays_per_s": round(rays / ms_batch * 1000.0, 1),
             "speedup": round(ms_plain / ms_batch, 3), "tuned": [list(v) for v in br.tuned.values()]}
+
+
+def differentiation_form(a, tracer, cam, target):
+    """The hand-written backward behind torch.autograd.Function (gray_gb300.autograd.render) on the
+    benchmark view: render + L1 + backward with the hit lists kept from the forward, and with them
+    recomputed by a second forward inside the backward (nothing kept between the two)."""
+    import torch
+    import torch.nn.functional as F
+
+    from gray_gb300.autograd import render
+
+    g = tracer.get_gaussians()
+    params = {k: getattr(g, k).detach().clone().requires_grad_() for k in
+              ("mean", "rotation", "scale", "opacity", "sh_coeffs_dc", "sh_coeffs_rest")}
+
+    def step(recompute):
+        img = render(tracer, cam, params["mean"], params["rotation"], params["scale"], params["opacity"],
+                     sh_dc=params["sh_coeffs_dc"], sh_rest=params["sh_coeffs_rest"], recompute=recompute)
+        F.l1_loss(img, target).backward()
+
+    out = {}
+    for mode, rc in (("stored_ms", False), ("recompute_ms", True)):
+        for _ in range(2):
+            step(rc)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            step(rc)
+        e1.record()
+        torch.cuda.synchronize()
+        out[mode] = round(e0.elapsed_time(e1) / 5, 3)
+    out["hitlist_mb"] = round(float(tracer.get_ppll_backward_data().total_hits.item()) * 4 / 1e6, 1)
+    tracer.check_status()
+    return out
 
 
 def served_form(a, rank):
