@@ -1383,7 +1383,8 @@ template <int KB, int MINB>
 __global__ void __launch_bounds__(kFwdThreads, MINB)
     trace_batch_kernel(const gray_batch_scene *__restrict__ scenes, const gray_batch_view *__restrict__ views,
                        int nviews, uint32_t total_packets, float *__restrict__ out, uint32_t *__restrict__ counter,
-                       int tile_w, const uint32_t *__restrict__ frontier, int32_t *status) {
+                       int tile_w, const uint32_t *__restrict__ frontier, uint32_t total_groups,
+                       int32_t *status) {
     __shared__ unsigned long long kbuf[KB][kFwdThreads];
     __shared__ Frustum sfr[kWarps];
     __shared__ uint32_t sstk[kWarps][kWideStack];
@@ -1435,7 +1436,8 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
         const uint32_t *front = nullptr;
         if (frontier) {
             const uint32_t tx = local % tiles_x, ty = local / tiles_x;
-            front = frontier + (size_t)(vw.group_offset + (ty / 2) * ((tiles_x + 1) / 2) + tx / 2) * kFrontierWords;
+            const uint32_t grp = vw.group_offset + (ty / 2) * ((tiles_x + 1) / 2) + tx / 2;
+            if (grp < total_groups) front = frontier + (size_t)grp * kFrontierWords;  // else: from the root
         }
         RayResult r;
         trace_ray<KB, (MINB < 6)>(sc, k, ro, rd, inside, false, hs, status, kbuf, r, &sfr[warp], sstk[warp], scand[warp],
@@ -1598,10 +1600,10 @@ cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_
     }
     const uint32_t *fr = frontier;
     switch (v & 3) {
-        case 0: trace_batch_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, status); break;
-        case 1: trace_batch_kernel<32, 4><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, status); break;
-        case 2: trace_batch_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, status); break;
-        default: trace_batch_kernel<16, 6><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, status); break;
+        case 0: trace_batch_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, total_groups, status); break;
+        case 1: trace_batch_kernel<32, 4><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, total_groups, status); break;
+        case 2: trace_batch_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, total_groups, status); break;
+        default: trace_batch_kernel<16, 6><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, total_groups, status); break;
     }
     return cudaGetLastError();
 }
