@@ -151,3 +151,36 @@ def test_maxalpha_product_is_correctly_rounded(oracle):
         ref = np.float32(0.9999 * float(a) * float(b))
         bad += lib.orc_maxalpha_mul(float(a), float(b)) != ref
     assert bad <= 2
+
+
+def test_lbvh_nodes_hold_their_leaf_counts(oracle):
+    """Node words 14 and 15 of the LBVH (the forward's frontier walk reads them instead of loading
+    the children): the leaves below the node and below its first child, consistent through the
+    whole tree and with every leaf below the root exactly once."""
+    from gray_gb300 import synthetic
+
+    sc = synthetic.clustered_scene(5000, seed=11)
+    _, _, aabb, vis = oracle.snapshot(sc.mean, sc.rotation, sc.scale, sc.opacity[:, 0])
+    tree = oracle.Bvh(aabb, vis)
+    nodes = tree.nodes
+    links = nodes[:, 12:14].copy().view(np.uint32)
+    counts = nodes[:, 14:16].copy().view(np.uint32)
+    leaf_bit = np.uint32(0x80000000)
+
+    def leaves(child):
+        return 1 if child & leaf_bit else int(counts[child, 0])
+
+    seen = []
+    stack = [0]
+    while stack:
+        i = stack.pop()
+        c0, c1 = int(links[i, 0]), int(links[i, 1])
+        assert counts[i, 1] == leaves(c0), i
+        assert counts[i, 0] == leaves(c0) + leaves(c1), i
+        for c in (c0, c1):
+            if c & leaf_bit:
+                seen.append(c & ~leaf_bit)
+            else:
+                stack.append(c)
+    assert counts[0, 0] == sc.n
+    assert sorted(seen) == list(range(sc.n))
