@@ -48,15 +48,19 @@ def test_errors_are_reported_without_a_gpu(gray_lib):
         _lib.call("gray_rebuild_bvh", p, 0)
 
 
-def _c_layout(tmp_path):
-    from gray_gb300 import _lib
+def _structs():
+    """(C struct name, ctypes mirror) of every struct the C ABI passes."""
+    from gray_gb300 import _lib, batch
 
+    return (("gray_gaussians", _lib.GaussiansC), ("gray_camera", _lib.CameraC), ("gray_config", _lib.ConfigC),
+            ("gray_framebuffer", _lib.FramebufferC), ("gray_metadata", _lib.MetadataC), ("gray_stats", _lib.StatsC),
+            ("gray_hitlist", _lib.HitlistC), ("gray_scene", _lib.SceneC), ("gray_params", _lib.ParamsC),
+            ("gray_batch_scene", batch.BatchSceneC), ("gray_batch_view", batch.BatchViewC))
+
+
+def _c_layout(tmp_path):
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', 'int main(void) {']
-    for cname, cls in (("gray_gaussians", _lib.GaussiansC), ("gray_camera", _lib.CameraC),
-                       ("gray_config", _lib.ConfigC), ("gray_framebuffer", _lib.FramebufferC),
-                       ("gray_metadata", _lib.MetadataC), ("gray_stats", _lib.StatsC),
-                       ("gray_hitlist", _lib.HitlistC), ("gray_scene", _lib.SceneC),
-                       ("gray_params", _lib.ParamsC)):
+    for cname, cls in _structs():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
         for f, _ in cls._fields_:
             lines.append(f'printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
@@ -70,14 +74,8 @@ def _c_layout(tmp_path):
 
 
 def test_ctypes_structs_match_c_layout(tmp_path):
-    from gray_gb300 import _lib
-
     c = _c_layout(tmp_path)
-    for cname, cls in (("gray_gaussians", _lib.GaussiansC), ("gray_camera", _lib.CameraC),
-                       ("gray_config", _lib.ConfigC), ("gray_framebuffer", _lib.FramebufferC),
-                       ("gray_metadata", _lib.MetadataC), ("gray_stats", _lib.StatsC),
-                       ("gray_hitlist", _lib.HitlistC), ("gray_scene", _lib.SceneC),
-                       ("gray_params", _lib.ParamsC)):
+    for cname, cls in _structs():
         assert int(c[f"{cname} size"]) == ctypes.sizeof(cls), cname
         for f, _ in cls._fields_:
             assert int(c[f"{cname}.{f}"]) == getattr(cls, f).offset, f"{cname}.{f}"
