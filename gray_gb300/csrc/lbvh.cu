@@ -5,11 +5,13 @@
 // sort of (code, gaussian id) with 8-bit digits (4 passes, no CUB) -> Karras (2012)
 // hierarchy, one thread per internal node -> bottom-up boxes.
 // Refit: bottom-up boxes only; each internal node is finished by the second of its two
-// children to arrive (one atomic counter per node, no spinning).
+// children to arrive (one visit counter per node, no spinning): first inside blocks of 256 sorted
+// leaves with shared-memory counters, then the upper tree from a queue of block-boundary nodes.
 //
 // Node layout (16 floats): child0 box (minx miny minz maxx maxy maxz), child1 box, child0 link,
-// child1 link, pad, pad.  A link with GRAY_LEAF_BIT set names a Gaussian; otherwise an
-// internal node.  Everything here is deterministic; the CPU oracle restates it bit-exactly.
+// child1 link, leaves below the node, leaves below child0 (both as uint32 bits).  A link with
+// GRAY_LEAF_BIT set names a Gaussian; otherwise an internal node.  Everything here is
+// deterministic; the CPU oracle restates it bit-exactly.
 #include "gray_device.cuh"
 #include "gray_internal.h"
 
