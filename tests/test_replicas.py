@@ -53,3 +53,25 @@ def test_two_gloo_replicas():
 def test_single_rank_is_unchanged():
     assert bench.max_over_ranks(12.5, 1, torch.device("cpu")) == 12.5
     assert bench.whole_job_rate(10, 100.0, 1) == pytest.approx(100.0)
+
+
+def test_reference_arm_json_line():
+    """The reference arm (the CPU restatement timed on the host) prints one JSON line with the
+    bench contract's keys, on the same metric, unit and workload as the GPU arm."""
+    import json
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--scene", "small",
+                          "--steps", "2", "--warmup", "1", "--cpu-sample-stride", "4"],
+                         capture_output=True, text=True, check=True, cwd=root, timeout=600).stdout
+    lines = [l for l in out.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == "train-steps/s"
+    assert d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 1 and d["higher_is_better"] is True
+    assert d["config"]["workload"] == "train step, 64 uniform [-1,1]^3 Gaussians, 256x256"
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": "train-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
