@@ -7,8 +7,8 @@ arguments, methods and tensor attributes (same shapes and dtypes, mutated in pla
 libgray_gb300.so through its C ABI instead of OptiX.  Code written against
 `torch.classes.gray.Raytracer(...)` works against `gray_gb300.classes.Raytracer(...)`.
 
-Differences that a caller can observe are listed in INTEGRATION.md (no forward per-pixel
-linked list is materialised; the backward hit list stores gaussian ids only).
+Differences a caller can observe: no forward per-pixel linked list is materialised (hits are
+selected during traversal), and the backward hit list stores gaussian ids only.
 """
 from __future__ import annotations
 
@@ -332,6 +332,8 @@ class Raytracer:
         self.schedule = torch.zeros(int(_lib.load().gray_schedule_words(self.width, self.height)), device=dev,
                                     dtype=torch.int32)
         self.trace_variant = 0  # forward-kernel variant (0 = library default); results do not depend on it
+        # counts forwards: each one overwrites the colours, saved state and hit lists a backward replays
+        self.generation = 0
         self._scene = _SceneWorkspace(1, dev, not self.inference_only)
         self._params = None
         if num_gaussians > 0:
@@ -381,9 +383,11 @@ class Raytracer:
     # ---- reference methods ----
     def forward_pass(self):
         self.meta_data.grads_enabled.fill_(torch.is_grad_enabled())
+        self.generation += 1
         self._call("gray_forward_pass")
 
     def forward_pass_display(self):
+        self.generation += 1
         self._call("gray_forward_pass_display")
 
     def backward_pass(self):

@@ -19,18 +19,12 @@ int fail(int code, const char *what) {
     return code;
 }
 
-int cuda_fail(cudaError_t e, const char *where) {
-    g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
-    return GRAY_ERR_CUDA;
-}
-
-
 bool frame_ok(const gray_params *p) {
     return p->render_width >= 1 && p->render_height >= 1 && p->render_width <= p->image_width &&
            p->render_height <= p->image_height;
 }
 
-int check_common(const gray_params *p) {
+int check_common_impl(const gray_params *p) {
     if (!p) return fail(GRAY_ERR_INVALID_ARGUMENT, "null params");
     if (p->gaussians.count < 0) return fail(GRAY_ERR_INVALID_ARGUMENT, "negative Gaussian count");
     if (!frame_ok(p))
@@ -43,7 +37,7 @@ int check_common(const gray_params *p) {
 }
 
 int check_trace(const gray_params *p) {
-    int e = check_common(p);
+    int e = check_common_impl(p);
     if (e) return e;
     if (p->gaussians.count > 0 && !p->scene.bvh_valid)
         return fail(GRAY_ERR_INVALID_ARGUMENT, "the BVH is stale: call rebuild_bvh after creating or resizing");
@@ -63,39 +57,36 @@ bool g_prof_on = false;
 std::vector<cudaEvent_t> g_prof_events;
 std::vector<ProfRecord> g_prof_records;
 
-struct ProfScope {
-    bool on;
-    cudaStream_t s;
-    ProfScope(const char *name, cudaStream_t stream) : on(g_prof_on), s(stream) {
-        if (!on) return;
-        int ev = (int)g_prof_records.size() * 2;
-        if (ev + 1 >= (int)g_prof_events.size()) {
-            on = false;  // pool exhausted: stop recording rather than allocate in a timed region
-            return;
-        }
-        g_prof_records.push_back(ProfRecord{name, ev});
-        cudaEventRecord(g_prof_events[ev], s);
-    }
-    ~ProfScope() {
-        if (on) cudaEventRecord(g_prof_events[g_prof_records.back().ev + 1], s);
-    }
-};
-
 }  // namespace
 
 namespace gray {
+
 void set_last_error(const char *what) { g_last_error = what; }
+
+int cuda_fail(cudaError_t e, const char *where) {
+    g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return GRAY_ERR_CUDA;
+}
+
+int check_common(const gray_params *p) { return check_common_impl(p); }
+
+ProfScope::ProfScope(const char *name, cudaStream_t s) : ev_(-1), s_(s) {
+    if (!g_prof_on) return;
+    const int ev = (int)g_prof_records.size() * 2;
+    if (ev + 1 >= (int)g_prof_events.size()) return;  // pool exhausted: stop recording rather than allocate
+    g_prof_records.push_back(ProfRecord{name, ev});
+    ev_ = ev;
+    cudaEventRecord(g_prof_events[ev], s_);
+}
+
+ProfScope::~ProfScope() {
+    if (ev_ >= 0) cudaEventRecord(g_prof_events[ev_ + 1], s_);
+}
+
 }  // namespace gray
 
-#define GRAY_LAUNCH(name, expr)                                      \
-    do {                                                             \
-        cudaError_t _e;                                              \
-        {                                                            \
-            ProfScope _ps(name, s);                                  \
-            _e = (expr);                                             \
-        }                                                            \
-        if (_e != cudaSuccess) return cuda_fail(_e, name);           \
-    } while (0)
+using gray::check_common;
+using gray::cuda_fail;
 
 extern "C" {
 
@@ -199,6 +190,10 @@ int gray_update_bvh(const gray_params *p, void *stream) {
     if (e) return e;
     if (p->gaussians.count > 0 && !p->scene.bvh_valid)
         return fail(GRAY_ERR_INVALID_ARGUMENT, "update_bvh before rebuild_bvh");
+    if (p->gaussians.count > 1 && !p->scene.refit_flags)
+        return fail(GRAY_ERR_INVALID_ARGUMENT,
+                    "update_bvh needs scene.refit_flags (one visit counter per internal node), also after "
+                    "gray_rebuild_bvh_static");
     cudaStream_t s = (cudaStream_t)stream;
     GRAY_LAUNCH("snapshot", gray::launch_snapshot(*p, s));
     GRAY_LAUNCH("refit", gray::launch_lbvh_refit(*p, s));

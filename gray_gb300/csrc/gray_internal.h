@@ -23,7 +23,15 @@ cudaError_t launch_batch_prep(const gray_params &p, const float *origins, int nv
 // lbvh.cu
 cudaError_t launch_lbvh_build(const gray_params &p, cudaStream_t s);
 cudaError_t launch_lbvh_refit(const gray_params &p, cudaStream_t s);
-size_t sort_tmp_words(int n);
+// radix sort: a block sorts a tile of kSortThreads x kSortItems keys
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+// sort scratch of a rebuild of n Gaussians: second key and value buffers, then 256 digit counts
+// per tile
+constexpr size_t sort_tmp_words(int n) {
+    return 2 * (size_t)n + 256 * (size_t)(n > 0 ? (n + kSortTile - 1) / kSortTile : 1);
+}
 
 // trace.cu
 // display: forward_pass_display (colour only; no hit lists or saved state, whatever grads_enabled holds)
@@ -42,6 +50,33 @@ cudaError_t launch_adam(const gray_params &p, cudaStream_t s);
 
 // capi.cu: message returned by gray_last_error() on this thread
 void set_last_error(const char *what);
+// capi.cu: sets the message and returns GRAY_ERR_CUDA
+int cuda_fail(cudaError_t e, const char *where);
+// capi.cu: argument checks every entry point makes (params present, sizes within range)
+int check_common(const gray_params *p);
+
+// capi.cu: records CUDA events around a launcher on its stream while gray_profiler_enable is on
+class ProfScope {
+  public:
+    ProfScope(const char *name, cudaStream_t s);
+    ~ProfScope();
+
+  private:
+    int ev_;
+    cudaStream_t s_;
+};
+
+// Run one launcher inside a profiler scope; return its error from the enclosing entry point.
+// Needs a cudaStream_t named `s` in scope.
+#define GRAY_LAUNCH(name, expr)                                            \
+    do {                                                                   \
+        cudaError_t _e;                                                    \
+        {                                                                  \
+            ::gray::ProfScope _ps(name, s);                                \
+            _e = (expr);                                                   \
+        }                                                                  \
+        if (_e != cudaSuccess) return ::gray::cuda_fail(_e, name);         \
+    } while (0)
 
 constexpr int kThreads = 256;
 inline unsigned int blocks_for(long long n, int threads = kThreads) {

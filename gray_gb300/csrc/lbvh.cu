@@ -99,15 +99,8 @@ __global__ void morton_kernel(int n, const float4 *__restrict__ aabb, const uint
 // Stable LSD radix sort, 8-bit digits.  A tile is kSortThreads x kSortItems keys processed in
 // kSortItems rounds of kSortThreads consecutive keys, so tile order == round-major order.
 // ---------------------------------------------------------------------------------------------
-constexpr int kSortThreads = 256;
-constexpr int kSortItems = 8;
-constexpr int kSortTile = kSortThreads * kSortItems;
+// (kSortThreads, kSortItems, kSortTile and sort_tmp_words are in gray_internal.h)
 constexpr int kSortWarps = kSortThreads / 32;
-
-size_t sort_tmp_words(int n) {
-    size_t tiles = (size_t)((n + kSortTile - 1) / kSortTile);
-    return 2 * (size_t)n + 256 * (tiles > 0 ? tiles : 1);
-}
 
 __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(int n, int shift, const uint32_t *__restrict__ keys,
                                                                  uint32_t *__restrict__ counts, int tiles) {
@@ -267,9 +260,16 @@ __device__ __forceinline__ uint32_t add_acq_rel(uint32_t *p, uint32_t v) {
     return old;
 }
 
+// A climb longer than any tree of 2^31 leaves can be (its parent links form a cycle or the
+// tree is corrupt) stops and reports instead of looping on.
+__device__ __forceinline__ void refit_gave_up(int32_t *status) {
+    if (status) atomicOr(status, GRAY_STATUS_REFIT_TIMEOUT);
+}
+
 __global__ void refit_kernel(int n, const float4 *__restrict__ aabb, const uint32_t *__restrict__ order,
                              const int32_t *__restrict__ leaf_parent, const int32_t *__restrict__ int_parent,
-                             float *__restrict__ nodes, uint32_t *__restrict__ flags, float *__restrict__ root_box) {
+                             float *__restrict__ nodes, uint32_t *__restrict__ flags, float *__restrict__ root_box,
+                             int32_t *__restrict__ status) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     uint32_t gid = order[k];
@@ -316,6 +316,7 @@ __global__ void refit_kernel(int n, const float4 *__restrict__ aabb, const uint3
         link = (uint32_t)p;
         p = pp;
     }
+    refit_gave_up(status);
 }
 
 __device__ __forceinline__ void write_root_box(float *root_box, const float box[6]) {
@@ -345,7 +346,8 @@ __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const floa
                                                                const int32_t *__restrict__ leaf_parent,
                                                                const int32_t *__restrict__ int_parent,
                                                                float *__restrict__ nodes, uint32_t *__restrict__ flags,
-                                                               uint32_t *__restrict__ queue, float *__restrict__ root_box) {
+                                                               uint32_t *__restrict__ queue, float *__restrict__ root_box,
+                                                               int32_t *__restrict__ status) {
     __shared__ uint32_t sflag[kThreads];
     __shared__ float sbox[kThreads][12];
     const int base = blockIdx.x * kThreads;
@@ -398,12 +400,13 @@ __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const floa
             return;
         }
     }
+    refit_gave_up(status);
 }
 
 __global__ void __launch_bounds__(kThreads) refit_top_kernel(const int32_t *__restrict__ int_parent,
                                                              float *__restrict__ nodes, uint32_t *__restrict__ flags,
                                                              const uint32_t *__restrict__ queue,
-                                                             float *__restrict__ root_box) {
+                                                             float *__restrict__ root_box, int32_t *__restrict__ status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= queue[0]) return;
     int p = (int)queue[1 + i];
@@ -426,6 +429,7 @@ __global__ void __launch_bounds__(kThreads) refit_top_kernel(const int32_t *__re
         if (add_acq_rel(&flags[pp], 1u) == 0u) return;
         p = pp;
     }
+    refit_gave_up(status);
 }
 
 cudaError_t launch_lbvh_refit(const gray_params &p, cudaStream_t s) {
@@ -444,14 +448,14 @@ cudaError_t launch_lbvh_refit(const gray_params &p, cudaStream_t s) {
         if ((e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
         refit_local_kernel<<<blocks, kThreads, 0, s>>>(n, reinterpret_cast<const float4 *>(sc.aabb), sc.order,
                                                        sc.leaf_parent, sc.int_parent, sc.nodes, sc.refit_flags, queue,
-                                                       sc.root_box);
+                                                       sc.root_box, p.status);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         refit_top_kernel<<<blocks_for(blocks), kThreads, 0, s>>>(sc.int_parent, sc.nodes, sc.refit_flags, queue,
-                                                                 sc.root_box);
+                                                                 sc.root_box, p.status);
         return cudaGetLastError();
     }
     refit_kernel<<<blocks, kThreads, 0, s>>>(n, reinterpret_cast<const float4 *>(sc.aabb), sc.order, sc.leaf_parent,
-                                             sc.int_parent, sc.nodes, sc.refit_flags, sc.root_box);
+                                             sc.int_parent, sc.nodes, sc.refit_flags, sc.root_box, p.status);
     return cudaGetLastError();
 }
 

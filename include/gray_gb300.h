@@ -274,10 +274,14 @@ int gray_profiler_collect(char *buf, size_t buflen);
  * and may be NULL.  The scratch is a fixed device array inside the library, sized for at most
  * GRAY_STATIC_MAX_GAUSSIANS Gaussians (about 3.3 MB, held by every device that loads the
  * library until the process exits); larger counts return GRAY_ERR_OUT_OF_RANGE.  The first call
- * on each device looks up that array's device address (cudaGetSymbolAddress, with the device
- * current), so make the first call before any stream capture.  Every call shares the one array:
- * calls whose work overlaps on the GPU (other streams, other threads) race and must be
- * serialised by the caller.  No allocation of any kind is made. */
+ * in each CUDA context (the device's primary context, or a driver-API context the caller made
+ * current) looks up that array's device address in that context (cudaGetSymbolAddress) and
+ * caches it under the context's id, so make the first call before any stream capture; a
+ * context re-created after cudaDeviceReset gets its own look-up.  Every call shares the one
+ * array: calls whose work overlaps on the GPU (other streams, other threads) race and must be
+ * serialised by the caller.  No allocation of any kind is made.  A later gray_update_bvh still
+ * needs the caller's scene.refit_flags (one visit counter per internal node): the array is the
+ * rebuild's only. */
 #define GRAY_STATIC_MAX_GAUSSIANS 262144
 int gray_rebuild_bvh_static(const gray_params *p, void *stream);
 

@@ -584,6 +584,54 @@ void orc_lbvh_refit(orc_bvh *b, const float *aabb) {
     b->root_box[3] = b->root_box[7] = 0.0f;
 }
 
+static void store_root_box(orc_bvh *b, const float box[6]) {
+    for (int k = 0; k < 3; k++) {
+        b->root_box[k] = box[k];
+        b->root_box[4 + k] = box[3 + k];
+    }
+    b->root_box[3] = b->root_box[7] = 0.0f;
+}
+
+int orc_lbvh_refit_climb(orc_bvh *b, const float *aabb) {
+    const int n = b->n;
+    if (n <= 0) return 0;
+    int status = 0;
+    uint32_t *flags = (uint32_t *)calloc((size_t)(n > 1 ? n - 1 : 1), sizeof(uint32_t));
+    for (int k = 0; k < n; k++) {
+        const uint32_t gid = b->order[k];
+        const float *a = aabb + 8 * (size_t)gid;
+        float box[6] = {a[0], a[1], a[2], a[4], a[5], a[6]};
+        int p = n > 1 ? b->leaf_parent[k] : -1;
+        if (p < 0) {
+            store_root_box(b, box);
+            continue;
+        }
+        uint32_t link = gid | LEAF_BIT;
+        int guard = 0;
+        for (; guard < 128; guard++) {
+            float *nd = b->nodes + 16 * (size_t)p;
+            uint32_t c0;
+            memcpy(&c0, nd + 12, 4);
+            memcpy(nd + 6 * (c0 == link ? 0 : 1), box, sizeof(box));
+            if (flags[p]++ == 0u) break;
+            for (int q = 0; q < 3; q++) {
+                box[q] = fminf(nd[q], nd[6 + q]);
+                box[3 + q] = fmaxf(nd[3 + q], nd[9 + q]);
+            }
+            const int pp = b->int_parent[p];
+            if (pp < 0) {
+                store_root_box(b, box);
+                break;
+            }
+            link = (uint32_t)p;
+            p = pp;
+        }
+        if (guard == 128) status |= 4;
+    }
+    free(flags);
+    return status;
+}
+
 void orc_lbvh_free(orc_bvh *b) {
     free(b->nodes);
     free(b->codes);

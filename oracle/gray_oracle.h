@@ -77,6 +77,12 @@ typedef struct {
 
 void orc_lbvh_build(int n, const float *aabb, const uint8_t *visible, orc_bvh *out);
 void orc_lbvh_refit(orc_bvh *bvh, const float *aabb);
+/* The GPU refit's bottom-up protocol (gray_gb300/csrc/lbvh.cu refit_kernel), one climber per sorted
+ * leaf run to completion in leaf order: a climber stores its box in its parent's slot and counts its
+ * visit; the first arriver stops, the second unions the two child boxes and climbs on.  A climb of
+ * more than 128 levels stops and sets bit 4 (GRAY_STATUS_REFIT_TIMEOUT) of the returned status.
+ * The parent links are bvh->int_parent / leaf_parent, so a caller can plant a corrupt chain. */
+int orc_lbvh_refit_climb(orc_bvh *bvh, const float *aabb);
 void orc_lbvh_free(orc_bvh *bvh);
 
 /* ---- trace forward (cuda/shaders.cu:10-67 + cuda/forward_pass.cu:6-151) ---- */

@@ -86,6 +86,8 @@ def lib():
                                       U8P, F32P, F32P, F32P]
         L.orc_lbvh_build.argtypes = [ctypes.c_int, F32P, U8P, ctypes.POINTER(_Bvh)]
         L.orc_lbvh_refit.argtypes = [ctypes.POINTER(_Bvh), F32P]
+        L.orc_lbvh_refit_climb.argtypes = [ctypes.POINTER(_Bvh), F32P]
+        L.orc_lbvh_refit_climb.restype = ctypes.c_int
         L.orc_lbvh_free.argtypes = [ctypes.POINTER(_Bvh)]
         L.orc_trace_forward.argtypes = [
             ctypes.c_int, F32P, F32P, ctypes.c_int, F32P, F32P, F32P, U8P, ctypes.c_void_p,
@@ -204,6 +206,19 @@ class Bvh:
 
     def refit(self, aabb):
         lib().orc_lbvh_refit(ctypes.byref(self._c), _f32(aabb))
+
+    def refit_climb(self, aabb) -> int:
+        """Bottom-up refit by the GPU's climbing protocol; returns its status bits."""
+        return int(lib().orc_lbvh_refit_climb(ctypes.byref(self._c), _f32(aabb)))
+
+    @property
+    def int_parent(self):
+        m = max(self.n - 1, 0)
+        return np.ctypeslib.as_array(self._c.int_parent, shape=(max(m, 1),))[:m]
+
+    @property
+    def leaf_parent(self):
+        return np.ctypeslib.as_array(self._c.leaf_parent, shape=(self.n,))
 
     @property
     def nodes(self):

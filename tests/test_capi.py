@@ -48,6 +48,19 @@ def test_errors_are_reported_without_a_gpu(gray_lib):
         _lib.call("gray_rebuild_bvh", p, 0)
 
 
+def test_refit_without_visit_counters_is_refused(gray_lib):
+    """A refit needs the caller's refit_flags (the static rebuild's scratch is its own): a NULL
+    pointer is an argument error, raised before any launch."""
+    from gray_gb300 import _lib
+
+    p = _lib.ParamsC()
+    p.image_width = p.image_height = p.render_width = p.render_height = 16
+    p.gaussians.count = 100
+    p.scene.bvh_valid = 1
+    with pytest.raises(_lib.GrayError, match="refit_flags"):
+        _lib.call("gray_update_bvh", p, 0)
+
+
 def _structs():
     """(C struct name, ctypes mirror) of every struct the C ABI passes."""
     from gray_gb300 import _lib, batch

@@ -184,3 +184,42 @@ def test_lbvh_nodes_hold_their_leaf_counts(oracle):
                 stack.append(c)
     assert counts[0, 0] == sc.n
     assert sorted(seen) == list(range(sc.n))
+
+
+def _random_tree(oracle, n, seed):
+    rng = np.random.default_rng(seed)
+    mean = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    rot = rng.standard_normal((n, 4)).astype(np.float32)
+    scale = rng.normal(-3, 0.3, (n, 3)).astype(np.float32)
+    opac = rng.standard_normal(n).astype(np.float32)
+    _, _, aabb, vis = oracle.snapshot(mean, rot, scale, opac)
+    return oracle.Bvh(aabb, vis), aabb, rng
+
+
+def test_refit_climb_equals_top_down_refit(oracle):
+    """The GPU refit's bottom-up protocol (visit counters, second arriver climbs on) gives the
+    top-down refit's node and root boxes, with no status bit, on trees of several sizes."""
+    for n in (1, 2, 3, 257, 1000):
+        tree, aabb, rng = _random_tree(oracle, n, n)
+        aabb2 = aabb.copy()
+        aabb2[:, :3] -= rng.uniform(0, 0.1, (n, 3)).astype(np.float32)
+        tree.refit(aabb2)
+        nodes, root = tree.nodes, tree.root_box
+        tree.refit(aabb)
+        assert tree.refit_climb(aabb2) == 0
+        assert np.array_equal(tree.nodes, nodes)
+        assert np.array_equal(tree.root_box, root)
+
+
+def test_refit_climb_reports_a_corrupt_parent_chain(oracle):
+    """A parent link that points back down the tree makes a cycle: the climb stops after 128 levels
+    and reports GRAY_STATUS_REFIT_TIMEOUT (bit 4) instead of looping (the mistake is planted in the
+    oracle's copy of the tree, on the CPU)."""
+    tree, aabb, _ = _random_tree(oracle, 1000, 7)
+    nodes = tree.nodes
+    links = nodes[:, 12:14].view(np.uint32)
+    internal = links[0][links[0] < 0x80000000]
+    assert internal.size > 0
+    child = int(internal[0])
+    tree.int_parent[0] = child  # the root's parent is now its own child
+    assert tree.refit_climb(aabb) & 4 == 4
