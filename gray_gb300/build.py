@@ -78,5 +78,38 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> str:
     return LIB
 
 
+TORCH_SRC = os.path.join(HERE, "torch_binding", "gray_torch.cpp")
+TORCH_LIB = os.path.join(BUILD, "libgray.so")
+
+
+def build_torch_binding(force: bool = False) -> str:
+    """Build libgray.so: torch.classes.gray.* (the reference's TorchScript classes) over the C ABI,
+    compiled with g++ against the installed torch and linked to libgray_gb300.so (found next to it)."""
+    import torch
+    from torch.utils import cpp_extension as ce
+
+    lib = build(force=force)
+    deps = [TORCH_SRC, lib, os.path.join(HERE, "..", "include", "gray_gb300.h")]
+    if not force and os.path.exists(TORCH_LIB) and all(os.path.getmtime(d) <= os.path.getmtime(TORCH_LIB)
+                                                        for d in deps):
+        return TORCH_LIB
+    cuda_home = os.path.dirname(os.path.dirname(nvcc()))
+    torch_lib = os.path.join(os.path.dirname(torch.__file__), "lib")
+    incs = [f"-I{p}" for p in ce.include_paths()] + [f"-I{os.path.join(cuda_home, 'include')}"]
+    abi = int(torch._C._GLIBCXX_USE_CXX11_ABI)
+    tmp = TORCH_LIB + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", f"-D_GLIBCXX_USE_CXX11_ABI={abi}", *incs, TORCH_SRC,
+           "-o", tmp, f"-L{torch_lib}", "-lc10", "-lc10_cuda", "-ltorch_cpu", "-ltorch",
+           f"-L{BUILD}", "-lgray_gb300", f"-L{os.path.join(cuda_home, 'lib64')}", "-lcudart",
+           "-Wl,-rpath,$ORIGIN", f"-Wl,-rpath,{torch_lib}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed for {TORCH_SRC}:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, TORCH_LIB)
+    return TORCH_LIB
+
+
 if __name__ == "__main__":
     print(build(verbose_ptxas="--verbose-ptxas" in sys.argv, force="--force" in sys.argv))
+    if "--torch-binding" in sys.argv:
+        print(build_torch_binding(force="--force" in sys.argv))

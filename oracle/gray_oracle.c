@@ -195,6 +195,8 @@ static inline float eval_gaussian(float d, float exp_power) {
     return orc_expf(-orc_powf(d, exp_power) / k);
 }
 
+float orc_eval_gaussian(float d, float exp_power) { return eval_gaussian(d, exp_power); }
+
 /* ------------------------------------------------------------------------------------------ */
 /* snapshot: cuda/optix/bvh_wrapper.cu:8-59                                                   */
 /* ------------------------------------------------------------------------------------------ */

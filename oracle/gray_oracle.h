@@ -37,6 +37,8 @@ uint16_t orc_f2h(float f);
 float orc_h2f(uint16_t h);
 float orc_scaling_factor(float opacity, float alpha_threshold, float exp_power);
 float orc_maxalpha_mul(float a, float b);
+/* Gaussian response at squared local radius d (cuda/utils/kernel.cu:24-38), as the GPU evaluates it */
+float orc_eval_gaussian(float d, float exp_power);
 float orc_adam_pow(float beta, int n);
 
 /* ---- per-Gaussian snapshot (populate_bvh_kernel, cuda/optix/bvh_wrapper.cu:8-59) ----

@@ -72,6 +72,8 @@ def lib():
         L.orc_h2f.restype = ctypes.c_float
         L.orc_h2f.argtypes = [ctypes.c_uint16]
         L.orc_maxalpha_mul.restype = ctypes.c_float
+        L.orc_eval_gaussian.restype = ctypes.c_float
+        L.orc_eval_gaussian.argtypes = [ctypes.c_float, ctypes.c_float]
         L.orc_maxalpha_mul.argtypes = [ctypes.c_float, ctypes.c_float]
         L.orc_adam_pow.restype = ctypes.c_float
         L.orc_adam_pow.argtypes = [ctypes.c_float, ctypes.c_int]
@@ -143,6 +145,15 @@ def expf(x: float) -> float:
 
 def logf(x: float) -> float:
     return lib().orc_logf(x)
+
+
+def eval_gaussian(d: float, exp_power=2.0) -> float:
+    """Response at squared local radius d, as the GPU evaluates it."""
+    return float(lib().orc_eval_gaussian(d, exp_power))
+
+
+def maxalpha_mul(a: float, b: float) -> float:
+    return float(lib().orc_maxalpha_mul(a, b))
 
 
 def scaling_factor(opacity: float, alpha_threshold=0.01, exp_power=2.0) -> float:
