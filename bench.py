@@ -55,6 +55,9 @@ def parse_args(argv):
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--no-served", action="store_true", help="skip the served measurement only")
     ap.add_argument("--trace-variant", type=int, default=0, help="forward-kernel variant (0 = library default)")
+    ap.add_argument("--record-traffic", nargs="+", metavar=("CSV", "KEY"),
+                    help="store the DRAM bytes of an ncu CSV capture (CSV KEY [UNITS_SCALE]) in "
+                         "profiles/ncu_traffic.json with the digest of the current kernel sources, and exit")
     ap.add_argument("--scene", default="clustered", choices=["clustered", "small", "gradcheck"],
                     help="clustered: --n-gaussians clustered Gaussians on a radius-8 orbit; small: 64 Gaussians in "
                          "[-1,1]^3, 256x256 camera at distance 4 (fx = 256); gradcheck: 1000 Gaussians in [-2,2]^3, "
@@ -203,14 +206,64 @@ def whole_job_rate(units_per_rank, ms, world):
     return units_per_rank * world / (ms / 1000.0)
 
 
+def kernel_source_hash() -> str:
+    """Digest of the CUDA sources (gray_gb300/csrc), to tie a captured DRAM figure to the kernels it
+    was measured on."""
+    import hashlib
+
+    h = hashlib.sha256()
+    csrc = os.path.join(ROOT, "gray_gb300", "csrc")
+    for name in sorted(os.listdir(csrc)):
+        if name.endswith((".cu", ".cuh", ".h")):
+            h.update(name.encode())
+            h.update(open(os.path.join(csrc, name), "rb").read())
+    return h.hexdigest()[:16]
+
+
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+
+
 def ncu_traffic(kernel, a):
     """DRAM bytes (read + write) of one launch of `kernel` on this workload, from an ncu capture
-    summarised in profiles/ncu_traffic.json (key "<kernel> <gaussians> <width>x<height>")."""
+    summarised in profiles/ncu_traffic.json (key "<kernel> <gaussians> <width>x<height>"); None when
+    the capture was made on other kernel sources than the ones built now."""
     try:
-        table = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
-        return table.get(f"{kernel} {a.n_gaussians} {a.width}x{a.height}")
+        entry = json.load(open(TRAFFIC_FILE)).get(f"{kernel} {a.n_gaussians} {a.width}x{a.height}")
     except Exception:
         return None
+    if not isinstance(entry, dict) or entry.get("sources") != kernel_source_hash():
+        return None
+    return entry.get("bytes")
+
+
+def record_traffic(csv_path, key, per_launch_units=1.0):
+    """Add the DRAM bytes of the kernel launches in an ncu CSV (--metrics dram__bytes_read.sum,
+    dram__bytes_write.sum --csv) to profiles/ncu_traffic.json under `key`, averaged per launch and
+    scaled by per_launch_units (a capture of a smaller case scaled to the full launch), together with
+    the digest of the kernel sources it was captured on."""
+    import csv
+
+    per_launch = {}
+    with open(csv_path) as f:
+        rows = [r for r in csv.reader(f) if r]
+    head = next(i for i, r in enumerate(rows) if "Metric Name" in r)
+    cols = rows[head]
+    mi, vi, ii = cols.index("Metric Name"), cols.index("Metric Value"), cols.index("ID")
+    units = rows[head + 1] if rows[head + 1][mi] == "" else None
+    for r in rows[head + 1 + (1 if units else 0):]:
+        if r[mi] in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+            v = float(r[vi].replace(",", ""))
+            unit = r[cols.index("Metric Unit")] if "Metric Unit" in cols else "byte"
+            v *= {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "KB": 1e3, "MB": 1e6, "GB": 1e9}.get(unit, 1)
+            per_launch[r[ii]] = per_launch.get(r[ii], 0.0) + v
+    avg = sum(per_launch.values()) / max(len(per_launch), 1) * per_launch_units
+    try:
+        table = json.load(open(TRAFFIC_FILE))
+    except Exception:
+        table = {}
+    table[key] = {"bytes": int(avg), "launches": len(per_launch), "sources": kernel_source_hash()}
+    json.dump(table, open(TRAFFIC_FILE, "w"), indent=1, sort_keys=True)
+    return table[key]
 
 
 def gpu_arm(a, rank, world, local_rank):
@@ -313,6 +366,7 @@ def gpu_arm(a, rank, world, local_rank):
     clocks.mark_end()
     clk = clocks.stop()
     rt.cuda_module.check_status()
+    V = float(rt.cuda_module.get_gaussians().was_visible.sum().item())  # Gaussians the last backward touched
     H = float(st.num_gaussians_hit.sum().item()) / a.steps
     A = float(st.num_gaussians_accumulated.sum().item()) / a.steps
     R = a.width * a.height
@@ -341,7 +395,10 @@ def gpu_arm(a, rank, world, local_rank):
         "trace_forward": 44.0 * H + 12.0 * A + 60.0 * R,
         "trace_backward": 120.0 * A + 72.0 * R,
         "forward_prep": 228.0 * n,
-        "fold_sh_backward": 460.0 * n,
+        # every accumulator row is read (64 B); rows of Gaussians the replay touched are cleared (64 B),
+        # folded into the gradients (read + write of 60 B), flagged visible (1 B), and run through the
+        # SH backward (mean 12, coefficients 180 + colour 12 read; grad_dc 12 + grad_rest 180 written)
+        "fold_sh_backward": 64.0 * n + (64.0 + 120.0 + 1.0 + 12.0 + 180.0 + 12.0 + 12.0 + 180.0) * V,
         "adam": (59 * 32.0 + 12.0) * n,  # 59 Adam floats x (p, m, v, g) read + written; channel grads zeroed
         "snapshot": (44.0 + 48 + 48 + 32) * n,
         "refit": 44.0 * n + 24.0 * (2 * n - 1),
@@ -357,14 +414,20 @@ def gpu_arm(a, rank, world, local_rank):
     launches = sum(cnt * kernels_per_group.get(name, 1) for name, (_, cnt) in res.items())
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "traffic": ncu_traffic(dominant, a), "algorithmic_bytes": algo.get(dominant),
+                "traffic": ncu_traffic(dominant, a), "traffic_sources": kernel_source_hash(),
+                "algorithmic_bytes": algo.get(dominant),
                 "avg_launch_ms": round(dom_ms, 4),
                 "shares": {k: round(v[0] / total_ms, 4) for k, v in sorted(res.items(), key=lambda kv: -kv[1][0])},
                 "hits_per_ray": round(H / R, 2), "composited_per_ray": round(A / R, 2)}
 
     batched = None if a.no_extras else batched_form(a, rt.cuda_module)
     differentiation = None if a.no_extras else differentiation_form(a, rt.cuda_module, cam, target_dev)
-    served = None if (a.no_extras or a.no_served) else served_form(a, rank)
+    served = None
+    if not (a.no_extras or a.no_served):
+        served = served_form(a, rank)  # the serving configuration's precision (fp32)
+        # the reference's inference mode (fp16 SH coefficients), continuous batching only
+        served["fp16_sh_variant"] = served_form(a, rank, sh_fp16=True, plain=False,
+                                                requests=max(a.serve_requests // 2, 1))
 
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
@@ -465,11 +528,14 @@ def differentiation_form(a, tracer, cam, target):
     return out
 
 
-def served_form(a, rank):
-    """Four resident inference scenes (0.5M, 1M, 3M, 6M clustered Gaussians, different seeds, fp16 SH);
-    Poisson arrivals at 200 req/s, each naming a scene, a random orbit pose and a resolution uniform in
-    {640x480, 1280x720, 1920x1080, 3840x2160}; continuous batching vs the plain one-request-per-launch
-    loop on the same schedule."""
+SERVE_SLOTS, SERVE_MAX_BATCH, SERVE_RAY_BUDGET = 2, 16, None
+
+
+def served_form(a, rank, sh_fp16=False, plain=True, requests=None, slots=None, max_batch=None, ray_budget=-1):
+    """Four resident inference scenes (0.5M, 1M, 3M, 6M clustered Gaussians, different seeds; fp32 SH,
+    or fp16 SH as the reference's inference mode stores it); Poisson arrivals at 200 req/s, each naming
+    a scene, a random orbit pose and a resolution uniform in {640x480, 1280x720, 1920x1080, 3840x2160};
+    continuous batching vs the plain one-request-per-launch loop on the same schedule."""
     import numpy as np
     import torch
 
@@ -480,7 +546,7 @@ def served_form(a, rank):
     tracers = []
     for i, n in enumerate(sizes):
         sc = synthetic.clustered_scene(n, seed=100 + i)
-        t = classes.Raytracer(3840, 2160, n, 3, 1, 1, inference_only=True)
+        t = classes.Raytracer(3840, 2160, n, 3, 1, 1, inference_only=True, inference_sh_fp16=sh_fp16)
         t.get_config().t_threshold.fill_(0.03)
         g = t.get_gaussians()
         with torch.no_grad():
@@ -493,7 +559,7 @@ def served_form(a, rank):
         del sc
     rng = np.random.default_rng(7 + rank)
     res = [(640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
-    count = a.serve_requests
+    count = requests or a.serve_requests
     sched = []
     for t_arr in poisson_arrivals(200.0, count, seed=3 + rank):
         w, h = res[int(rng.integers(0, 4))]
@@ -506,20 +572,28 @@ def served_form(a, rank):
         warm.submit(s_, cam)
     warm.drain()
     torch.cuda.synchronize()
-    srv = RenderServer(tracers, slots=2, max_batch=16)
+    slots = slots or SERVE_SLOTS
+    max_batch = max_batch or SERVE_MAX_BATCH
+    ray_budget = SERVE_RAY_BUDGET if ray_budget == -1 else ray_budget
+    srv = RenderServer(tracers, slots=slots, max_batch=max_batch, ray_budget=ray_budget)
     tuned = srv.tune([(s_, cam) for _, s_, cam in sched[:16]])
     reqs, wall = run_served(srv, sched)
     lat = np.array([r.latency for r in reqs]) * 1000.0
     rays = sum(r.rays for r in reqs)
-    plain, wall_p = plain_loop(tracers, sched)
-    lat_p = np.array([l for l, _ in plain]) * 1000.0
-    out = {"requests": count, "rate_hz": 200.0, "scenes": sizes,
+    out = {"dtype": "f16 SH" if sh_fp16 else "f32", "requests": count, "rate_hz": 200.0, "scenes": sizes,
+           "slots": slots, "max_batch": max_batch, "ray_budget": ray_budget,
            "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
-           "rays_per_s": round(rays / wall, 1),
-           "plain_p50_ms": round(float(np.percentile(lat_p, 50)), 2),
-           "plain_p99_ms": round(float(np.percentile(lat_p, 99)), 2),
-           "plain_rays_per_s": round(rays / wall_p, 1), "offered_rays_per_s": round(rays / sched[-1][0], 1),
-           "tuned": list(tuned)}
+           "rays_per_s": round(rays / wall, 1), "offered_rays_per_s": round(rays / sched[-1][0], 1),
+           "tuned": list(tuned),
+           "by_resolution": {f"{w}x{h}": {"p50_ms": round(float(np.percentile(v, 50)), 2),
+                                          "p99_ms": round(float(np.percentile(v, 99)), 2), "requests": len(v)}
+                             for (w, h) in res
+                             for v in [[r.latency * 1000.0 for r in reqs if r.camera.image_width == w]] if v}}
+    if plain:
+        plain_lat, wall_p = plain_loop(tracers, sched)
+        lat_p = np.array([l for l, _ in plain_lat]) * 1000.0
+        out.update(plain_p50_ms=round(float(np.percentile(lat_p, 50)), 2),
+                   plain_p99_ms=round(float(np.percentile(lat_p, 99)), 2), plain_rays_per_s=round(rays / wall_p, 1))
     del tracers
     torch.cuda.empty_cache()
     return out
@@ -528,8 +602,31 @@ def served_form(a, rank):
 # ----------------------------------------------------------------------------------------------
 # CPU restatement (oracle): baseline leg and reference arm
 # ----------------------------------------------------------------------------------------------
+def cpu_model() -> str:
+    """The host CPU's model name (x86 'model name', or lscpu's 'Model name' on Arm)."""
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
 class CpuScene:
-    """The oracle's view of the benchmark scene: snapshot, BVH, SH colours, sample rays."""
+    """The oracle's view of the benchmark scene: snapshot, BVH, SH colours, sample rays, and a slice
+    of the Gaussians with its own BVH for the per-Gaussian passes."""
+
+    SLICE = 200_000
 
     def __init__(self, a, sc, cam):
         import numpy as np
@@ -541,24 +638,35 @@ class CpuScene:
         self.a = a
         self.threads = O.hardware_threads()
         self.sc = sc
+        self.origin = cam.origin.astype(np.float32)
         self.geom, self.l2w, self.aabb, self.vis = O.snapshot(sc.mean, sc.rotation, sc.scale, sc.opacity[:, 0])
         self.live = O.forward_prep(sc.opacity[:, 0])
-        self.chan = O.sh_forward(3, sc.mean, cam.origin.astype(np.float32), sc.sh_dc[:, 0, :], sc.sh_rest)
+        self.chan = O.sh_forward(3, sc.mean, self.origin, sc.sh_dc[:, 0, :], sc.sh_rest)
         self.bvh = O.Bvh(self.aabb, self.vis)
-        ro, rd = O.camera_rays(a.width, a.height, cam.fov_y, cam.origin.astype(np.float32), cam.rotation_c2w_blender())
+        ro, rd = O.camera_rays(a.width, a.height, cam.fov_y, self.origin, cam.rotation_c2w_blender())
         s = a.cpu_sample_stride
         ys, xs = np.meshgrid(np.arange(s // 2, a.height, s), np.arange(s // 2, a.width, s), indexing="ij")
         idx = (ys * a.width + xs).ravel()
         self.ro, self.rd = ro[idx], rd[idx]
         self.cfg = O.TraceConfig(t_threshold=0.03)
-        self.rng = np.random.default_rng(0)
+        m = self.m = min(sc.n, self.SLICE)
+        self.slice_bvh = O.Bvh(self.aabb[:m], self.vis[:m])
+        self.state = {}
+        for name, width in (("channels", 3), ("opacity", 1), ("mean", 3), ("rotation", 4), ("scale", 3),
+                            ("sh_dc", 3), ("sh_rest", 45)):
+            for pre in ("", "g_", "m_", "v_"):
+                self.state[pre + name] = np.zeros(m * width, np.float32)
+        self.ray_fraction = self.ro.shape[0] / float(a.width * a.height)
+        self.gauss_fraction = m / float(sc.n)
 
     def step_seconds(self):
-        """One extrapolated CPU train step: trace forward + backward on the ray sample scaled to the
-        full image, plus SH, Adam, snapshot and refit over a slice of the Gaussians scaled to N."""
+        """One extrapolated CPU train step: trace forward + backward on the ray sample (all threads)
+        scaled to the full image, plus SH forward and backward, Adam, snapshot and refit over a slice
+        of the Gaussians (one thread, as the oracle runs them) scaled to N.  Returns (extrapolated
+        seconds, seconds actually spent, forward result)."""
         import numpy as np
 
-        O, a, sc = self.O, self.a, self.sc
+        O, a, sc, m = self.O, self.a, self.sc, self.m
         R_full = a.width * a.height
         t0 = time.perf_counter()
         fwd = O.trace_forward(self.ro, self.rd, self.geom, self.live, self.chan, self.vis, self.cfg, bvh=self.bvh,
@@ -567,54 +675,80 @@ class CpuScene:
         O.trace_backward(a.width, a.height, self.ro, self.rd, fwd, gout, self.geom, self.l2w, sc.opacity, sc.scale,
                          sc.rotation, self.chan, self.cfg, nthreads=self.threads)
         t_trace = time.perf_counter() - t0
-        # per-Gaussian work on a slice (single thread), scaled to N
-        m = min(sc.n, 200_000)
         t1 = time.perf_counter()
-        O.sh_forward(3, sc.mean[:m], np.zeros(3, np.float32), sc.sh_dc[:m, 0, :], sc.sh_rest[:m])
-        st = {}
-        for name, width in (("channels", 3), ("opacity", 1), ("mean", 3), ("rotation", 4), ("scale", 3),
-                            ("sh_dc", 3), ("sh_rest", 45)):
-            for pre in ("", "g_", "m_", "v_"):
-                st[pre + name] = np.zeros(m * width, np.float32)
-        O.adam_step(st, {"mean": 1e-4}, m, 15, 1)
-        g2, l2, aabb2, vis2 = O.snapshot(sc.mean[:m], sc.rotation[:m], sc.scale[:m], sc.opacity[:m, 0])
-        t_gauss = (time.perf_counter() - t1) * (sc.n / m)
-        return t_trace * (R_full / self.ro.shape[0]) + t_gauss, fwd
+        chan = O.sh_forward(3, sc.mean[:m], self.origin, sc.sh_dc[:m, 0, :], sc.sh_rest[:m])
+        O.sh_backward(3, sc.mean[:m], self.origin, sc.sh_rest[:m], chan, chan, np.ones(m, np.uint8),
+                      np.zeros((m, 3), np.float32))
+        O.adam_step(self.state, {"mean": 1e-4}, m, 15, 1)
+        _, _, aabb2, _ = O.snapshot(sc.mean[:m], sc.rotation[:m], sc.scale[:m], sc.opacity[:m, 0])
+        self.slice_bvh.refit(aabb2)
+        t_gauss = time.perf_counter() - t1
+        spent = time.perf_counter() - t0
+        return t_trace / self.ray_fraction + t_gauss / self.gauss_fraction, spent, fwd
+
+    def measure(self, steps, warmup):
+        """The protocol both CPU figures use: `warmup` untimed steps, then the median of `steps`."""
+        for _ in range(warmup):
+            self.step_seconds()
+        runs = [self.step_seconds() for _ in range(steps)]
+        ext = statistics.median(r[0] for r in runs)
+        return ext, sum(r[1] for r in runs), runs[-1][2]
+
+    def describe(self, steps, timed_s):
+        a = self.a
+        return {"cores": self.threads, "cpu": cpu_model(), "kind": "port", "extrapolated": True,
+                "sampled_fraction": {"rays": round(self.ray_fraction, 6), "gaussians": round(self.gauss_fraction, 6)},
+                "timed_seconds": round(timed_s, 4), "timed_steps": steps,
+                "sample": f"per step: {self.ro.shape[0]} rays (1 per {a.cpu_sample_stride}^2 pixels) traced forward + "
+                          f"backward with the oracle's BVH on {self.threads} threads, scaled to {a.width}x{a.height}; "
+                          f"SH forward + backward, Adam, snapshot and refit on a {self.m}-Gaussian slice (1 thread), "
+                          f"scaled to {a.n_gaussians}; median of {steps} steps after warm-up"}
+
+
+CPU_BASELINE_STEPS, CPU_BASELINE_WARMUP = 3, 1
 
 
 def cpu_baseline(a, sc, cam):
     cs = CpuScene(a, sc, cam)
-    t, fwd = cs.step_seconds()
-    return {"value": round(1.0 / t, 5), "unit": "train-steps/s", "cores": cs.threads, "kind": "port",
-            "sample": f"{cs.ro.shape[0]} rays (1 per {a.cpu_sample_stride}^2 pixels) traced forward+backward with the "
-                      f"oracle's BVH on {cs.threads} threads, scaled to {a.width}x{a.height}; SH/Adam/snapshot on "
-                      f"a 200k-Gaussian slice scaled to {a.n_gaussians}",
-            "hits_per_ray_sample": round(float(fwd["nhit"].mean()), 2)}
+    t, spent, fwd = cs.measure(CPU_BASELINE_STEPS, CPU_BASELINE_WARMUP)
+    out = {"value": round(1.0 / t, 5), "unit": "train-steps/s"}
+    out.update(cs.describe(CPU_BASELINE_STEPS, spent))
+    out["hits_per_ray_sample"] = round(float(fwd["nhit"].mean()), 2)
+    return out
 
 
 def reference_arm(a, rank, world):
+    """The reference's algorithm on the host cores (the CPU restatement in oracle/; the reference
+    itself needs OptiX 8 and RT cores, which GB300 does not have), on the GPU arm's workload, under
+    the same protocol as the GPU arm's cpu_baseline.  Each step is a bounded sample of the step,
+    extrapolated: ms_per_step is the extrapolated full step, timed_seconds what the run spent."""
     if rank != 0:
         return None
     sc = make_scene(a)
     cam = make_camera(a, 0)
     cs = CpuScene(a, sc, cam)
-    for _ in range(a.warmup):
-        cs.step_seconds()
-    times = [cs.step_seconds()[0] for _ in range(a.steps)]
-    t = sum(times) / len(times)
+    t, spent, _ = cs.measure(a.steps, a.warmup)
     v = round(1.0 / t, 5)
+    base = {"value": v, "unit": "train-steps/s"}
+    base.update(cs.describe(a.steps, spent))
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "train-steps/s", "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1000 * t, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded {a.scene} scene)",
-            "config": dict(workload_config(a), parallelism="cpu"),
-            "cpu_baseline": {"value": v, "unit": "train-steps/s", "cores": cs.threads, "kind": "port",
-                             "sample": f"per step {cs.ro.shape[0]} rays forward+backward + 200k-Gaussian slice, "
-                                       "extrapolated to the full step; the reference (OptiX 8) does not build here"},
+            "config": dict(workload_config(a), parallelism=f"replicas x{world}"), "extrapolated": True,
+            "timed_seconds": round(spent, 4),
+            "note": "ms_per_step is the extrapolated full step; each timed step traced a sample of it "
+                    "(sampled_fraction), so steps x ms_per_step exceeds timed_seconds",
+            "cpu_baseline": base,
             "e2e": {"value": v, "unit": "train-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():
     a = parse()
+    if a.record_traffic:
+        csv_path, key = a.record_traffic[0], " ".join(a.record_traffic[1:2])
+        scale = float(a.record_traffic[2]) if len(a.record_traffic) > 2 else 1.0
+        print(json.dumps({key: record_traffic(csv_path, key, scale)}))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -105,14 +105,16 @@ class GaussianDataHolder:
     All tensors start with one row and are grown or shrunk in place by resize(); gradients are
     also exposed as the parameters' `.grad` like the reference's mutable_grad()."""
 
-    def __init__(self, max_sh_degree: int, inference_only: bool, device):
+    def __init__(self, max_sh_degree: int, inference_only: bool, device, inference_sh_fp16: bool = True):
         self.device = device
         self.count = 1
         self.max_sh_degree = int(max_sh_degree)
         self.num_sh_coeffs = (self.max_sh_degree + 1) ** 2 - 1
         self.inference_only = bool(inference_only)
         f = dict(device=device, dtype=torch.float32)
-        sh_dtype = torch.float16 if inference_only else torch.float32
+        # the reference stores SH in fp16 for inference (cuda/core/gaussians.h:132); inference_sh_fp16=False
+        # keeps fp32 coefficients in an inference holder (no gradients or optimiser state either way)
+        sh_dtype = torch.float16 if inference_only and inference_sh_fp16 else torch.float32
         self.current_sh_degree = torch.tensor([0], device=device, dtype=torch.int32)
         self.mean = torch.zeros(1, 3, **f)
         self.rotation = torch.zeros(1, 4, **f)
@@ -197,7 +199,7 @@ class GaussianDataHolder:
         g.count = self.count
         g.max_sh_degree = self.max_sh_degree
         g.num_sh_coeffs = self.num_sh_coeffs
-        g.sh_is_fp16 = int(self.inference_only)
+        g.sh_is_fp16 = int(self.sh_coeffs_dc.dtype == torch.float16)
         g.current_sh_degree = _p(self.current_sh_degree)
         for name in _PARAM_NAMES:
             setattr(g, name, _p(getattr(self, name)))
@@ -309,7 +311,7 @@ class Raytracer:
     """cuda/raytracer.h:29-184: torch.classes.gray.Raytracer over libgray_gb300.so."""
 
     def __init__(self, width: int, height: int, num_gaussians: int, sh_max_degree: int, ppll_forward_size: int,
-                 ppll_backward_size: int, inference_only: bool = False):
+                 ppll_backward_size: int, inference_only: bool = False, inference_sh_fp16: bool = True):
         _lib.load()
         dev = _dev()
         self.device = dev
@@ -321,7 +323,7 @@ class Raytracer:
         self.camera_data = CameraDataHolder(dev)
         self.config_data = ConfigDataHolder(dev)
         self.framebuffer_data = Framebuffer(self.width, self.height, dev)
-        self.gaussian_data = GaussianDataHolder(sh_max_degree, inference_only, dev)
+        self.gaussian_data = GaussianDataHolder(sh_max_degree, inference_only, dev, inference_sh_fp16)
         self.meta_data = MetaDataHolder(dev)
         self.stats_data = StatsDataHolder(self.width, self.height, dev)
         self.ppll_forward_data = PPLLDataHolder("forward", self.width, self.height, 1, dev)

@@ -28,9 +28,9 @@ constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;
 // sort scratch of a rebuild of n Gaussians: second key and value buffers, then 256 digit counts
-// per tile
+// per tile, then the 256 digit totals
 constexpr size_t sort_tmp_words(int n) {
-    return 2 * (size_t)n + 256 * (size_t)(n > 0 ? (n + kSortTile - 1) / kSortTile : 1);
+    return 2 * (size_t)n + 256 * (size_t)(n > 0 ? (n + kSortTile - 1) / kSortTile : 1) + 256;
 }
 
 // trace.cu

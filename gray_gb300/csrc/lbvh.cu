@@ -31,18 +31,26 @@ __global__ void bounds_init_kernel(uint32_t *bounds) {
     else if (t < 6) bounds[t] = 0u;
 }
 
-__global__ void bounds_kernel(int n, const float4 *__restrict__ aabb, uint32_t *__restrict__ bounds) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Scene bounds of the leaf-box centroids (finite ones only).  A grid-stride loop keeps each thread's
+// min/max in registers; warps and then the block reduce them, and one thread per block folds the
+// block's six values into the six global words (order-preserving encodings, so integer atomics do
+// float min/max).  min/max are exact, so the result does not depend on the order of the work.
+constexpr int kBoundsThreads = 256;
+constexpr int kBoundsMaxBlocks = 1216;
+
+__global__ void __launch_bounds__(kBoundsThreads) bounds_kernel(int n, const float4 *__restrict__ aabb,
+                                                                uint32_t *__restrict__ bounds) {
+    __shared__ float part[kBoundsThreads / 32][6];
     float lo[3] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000)};
     float hi[3] = {__int_as_float(0xff800000), __int_as_float(0xff800000), __int_as_float(0xff800000)};
-    if (i < n) {
-        float4 a = aabb[2 * i], b = aabb[2 * i + 1];
-        float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = aabb[2 * i], b = aabb[2 * i + 1];
+        const float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
         if (isfinite(c[0]) && isfinite(c[1]) && isfinite(c[2])) {
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-                lo[k] = c[k];
-                hi[k] = c[k];
+                lo[k] = fminf(lo[k], c[k]);
+                hi[k] = fmaxf(hi[k], c[k]);
             }
         }
     }
@@ -54,7 +62,24 @@ __global__ void bounds_kernel(int n, const float4 *__restrict__ aabb, uint32_t *
             hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], off));
         }
     }
-    if ((threadIdx.x & 31) == 0) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            part[warp][k] = lo[k];
+            part[warp][3 + k] = hi[k];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int w = 1; w < kBoundsThreads / 32; w++) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                lo[k] = fminf(lo[k], part[w][k]);
+                hi[k] = fmaxf(hi[k], part[w][3 + k]);
+            }
+        }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             if (lo[k] <= hi[k]) {
@@ -117,28 +142,47 @@ __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(int n, int shi
     counts[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// exclusive scan of counts[256 * tiles] (digit-major) by one block
-__global__ void __launch_bounds__(1024) radix_scan_kernel(uint32_t *__restrict__ counts, int total) {
-    __shared__ uint32_t part[1024];
-    const int t = threadIdx.x;
-    const int chunk = (total + 1023) / 1024;
-    const int b = t * chunk, e = min(b + chunk, total);
-    uint32_t s = 0;
-    for (int i = b; i < e; i++) s += counts[i];
-    part[t] = s;
+// Exclusive scan of each digit's row of tile counts (counts is digit-major: counts[d * tiles + tile]),
+// one block per digit, coalesced; the row's total goes to totals[d].  The scatter kernel adds each
+// digit's base (the exclusive scan of the 256 totals) itself.
+constexpr int kScanThreads = 512;
+
+__global__ void __launch_bounds__(kScanThreads) radix_row_scan_kernel(uint32_t *__restrict__ counts, int tiles,
+                                                                      uint32_t *__restrict__ totals) {
+    __shared__ uint32_t wsum[kScanThreads / 32];
+    __shared__ uint32_t carry;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint32_t *row = counts + (size_t)blockIdx.x * tiles;
+    if (t == 0) carry = 0u;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        uint32_t v = t >= off ? part[t - off] : 0u;
+    for (int c0 = 0; c0 < tiles; c0 += kScanThreads) {
+        const int i = c0 + t;
+        const uint32_t v = i < tiles ? row[i] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
         __syncthreads();
-        part[t] += v;
+        if (warp == 0) {
+            uint32_t w = lane < kScanThreads / 32 ? wsum[lane] : 0u;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= off) w += y;
+            }
+            if (lane < kScanThreads / 32) wsum[lane] = w;  // inclusive over warps
+        }
+        __syncthreads();
+        const uint32_t before = carry + (warp > 0 ? wsum[warp - 1] : 0u);
+        if (i < tiles) row[i] = before + x - v;
+        __syncthreads();
+        if (t == 0) carry += wsum[kScanThreads / 32 - 1];
         __syncthreads();
     }
-    uint32_t run = part[t] - s;
-    for (int i = b; i < e; i++) {
-        uint32_t c = counts[i];
-        counts[i] = run;
-        run += c;
-    }
+    if (t == 0) totals[blockIdx.x] = carry;
 }
 
 __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(int n, int shift,
@@ -146,13 +190,28 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(int n, int 
                                                                     const uint32_t *__restrict__ vals_in,
                                                                     uint32_t *__restrict__ keys_out,
                                                                     uint32_t *__restrict__ vals_out,
-                                                                    const uint32_t *__restrict__ offsets, int tiles) {
+                                                                    const uint32_t *__restrict__ offsets, int tiles,
+                                                                    const uint32_t *__restrict__ totals) {
     __shared__ uint32_t warp_cnt[kSortWarps][256];
     __shared__ uint32_t digit_run[256];
     __shared__ uint32_t digit_off[256];
+    __shared__ uint32_t wsum[kSortWarps];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     digit_run[t] = 0;
-    digit_off[t] = offsets[t * tiles + blockIdx.x];
+    {   // digit t's base: exclusive scan of the 256 digit totals (one per thread)
+        const uint32_t v = totals[t];
+        uint32_t x = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        uint32_t before = 0u;
+        for (int w = 0; w < warp; w++) before += wsum[w];
+        digit_off[t] = before + x - v + offsets[t * tiles + blockIdx.x];
+    }
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     const int base = blockIdx.x * kSortTile;
     for (int r = 0; r < kSortItems; r++) {
@@ -332,15 +391,19 @@ __device__ __forceinline__ void write_root_box(float *root_box, const float box[
 
 // Two-phase refit.  Phase 1: a block takes kThreads consecutive sorted leaves and climbs, as
 // refit_kernel does, through the internal nodes whose leaf range lies inside the block's (a Karras
-// node's index is one end of its range, so a local node's index is inside the block too): visit
-// counters and the sibling's box are in shared memory, so most of the tree is built without a
-// global atomic.  A climber tracks its subtree's leaf range [lo, hi]; a parent reached through
-// child 0 covers [lo, lo + leaves - 1], through child 1 [hi - leaves + 1, hi].  At the first node
-// whose range crosses the block's edge the climber stores its box and counts its visit in global
-// memory; the second arriver there appends the node to a queue (at most one node per block
-// boundary: the one that splits it) instead of climbing on, so no block stays resident for a long
-// climb.  Phase 2: one thread per queued node climbs the rest of the tree with the global protocol.
-// Boxes are min/max unions, so the result does not depend on the order of the work.
+// node's index is one end of its range, so a local node's index is inside the block too).  The block
+// first loads the link / leaf-count words (node words 12-15) and the parents of the nodes indexed
+// base .. base + kThreads - 1 into shared memory, so the local climb makes no dependent global loads;
+// visit counters and the first arriver's box are in shared memory too, and the second arriver writes
+// the whole 64-byte node (both child boxes and the unchanged link words): full 32-byte sectors, no
+// partial-sector writes for the memory system to merge.  A climber tracks its subtree's leaf range
+// [lo, hi]; a parent reached through child 0 covers [lo, lo + leaves - 1], through child 1
+// [hi - leaves + 1, hi].  At the first node whose range crosses the block's edge the climber stores
+// its box in the node and counts its visit in global memory; the second arriver there appends the
+// node to a queue (at most one node per block boundary: the one that splits it) instead of climbing
+// on, so no block stays resident for a long climb.  Phase 2: one thread per queued node climbs the
+// rest of the tree with the global protocol.  Boxes are min/max unions, so the result does not
+// depend on the order of the work.
 __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const float4 *__restrict__ aabb,
                                                                const uint32_t *__restrict__ order,
                                                                const int32_t *__restrict__ leaf_parent,
@@ -349,11 +412,18 @@ __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const floa
                                                                uint32_t *__restrict__ queue, float *__restrict__ root_box,
                                                                int32_t *__restrict__ status) {
     __shared__ uint32_t sflag[kThreads];
-    __shared__ float sbox[kThreads][12];
+    __shared__ float sbox[kThreads][6];  // the first arriver's box at each local node
+    __shared__ uint4 stopo[kThreads];    // node words 12-15 of the nodes base .. base + kThreads - 1
+    __shared__ int32_t spar[kThreads];   // their parents
     const int base = blockIdx.x * kThreads;
-    sflag[threadIdx.x] = 0u;
+    const int t = threadIdx.x;
+    sflag[t] = 0u;
+    if (base + t < n - 1) {
+        stopo[t] = __ldcg(reinterpret_cast<const uint4 *>(nodes) + 4 * (size_t)(base + t) + 3);
+        spar[t] = int_parent[base + t];
+    }
     __syncthreads();
-    const int k = base + threadIdx.x;
+    const int k = base + t;
     if (k >= n) return;
     const uint32_t gid = order[k];
     const float4 a = aabb[2 * gid], b = aabb[2 * gid + 1];
@@ -366,30 +436,48 @@ __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const floa
     int lo = k, hi = k;
     uint32_t link = gid | GRAY_LEAF_BIT;
     for (int guard = 0; guard < 128; guard++) {
-        // the parent's links and its own parent, loaded together (one round trip per level)
-        const float4 q3 = __ldcg(reinterpret_cast<const float4 *>(nodes) + 4 * (size_t)p + 3);
-        const int pnext = int_parent[p];
-        const int slot = __float_as_uint(q3.x) == link ? 0 : 1;
-        const int leaves = (int)__float_as_uint(q3.z);
+        const bool in_block = p >= base && p < base + kThreads;
+        uint4 q3;
+        int pnext;
+        if (in_block) {
+            q3 = stopo[p - base];
+            pnext = spar[p - base];
+        } else {
+            q3 = __ldcg(reinterpret_cast<const uint4 *>(nodes) + 4 * (size_t)p + 3);
+            pnext = int_parent[p];
+        }
+        const int slot = q3.x == link ? 0 : 1;
+        const int leaves = (int)q3.z;
         const int plo = slot == 0 ? lo : hi - leaves + 1, phi = slot == 0 ? lo + leaves - 1 : hi;
-        store_child_box(nodes, p, slot, box);
         if (plo < base || phi >= base + kThreads) {
-            // the parent's range leaves the block: global counter, then phase 2
+            // the parent's range leaves the block: box into the node, global counter, then phase 2
+            store_child_box(nodes, p, slot, box);
             if (add_acq_rel(&flags[p], 1u) == 0u) return;
             const uint32_t at = atomicAdd(queue, 1u);
             queue[1 + at] = (uint32_t)p;
             return;
         }
+        // p is local (its range lies inside the block, and p is one end of it)
         float *sb = sbox[p - base];
 #pragma unroll
-        for (int q = 0; q < 6; q++) sb[6 * slot + q] = box[q];
+        for (int q = 0; q < 6; q++) sb[q] = box[q];
         __threadfence_block();
         if (atomicAdd(&sflag[p - base], 1u) == 0u) return;
         __threadfence_block();
+        float sib[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) sib[q] = sb[q];
+        const float *c0 = slot == 0 ? box : sib, *c1 = slot == 0 ? sib : box;
+        float4 *nd = reinterpret_cast<float4 *>(nodes) + 4 * (size_t)p;
+        __stcg(nd, make_float4(c0[0], c0[1], c0[2], c0[3]));
+        __stcg(nd + 1, make_float4(c0[4], c0[5], c1[0], c1[1]));
+        __stcg(nd + 2, make_float4(c1[2], c1[3], c1[4], c1[5]));
+        __stcg(nd + 3, make_float4(__uint_as_float(q3.x), __uint_as_float(q3.y), __uint_as_float(q3.z),
+                                   __uint_as_float(q3.w)));
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            box[q] = fminf(box[q], sb[6 * (1 - slot) + q]);
-            box[3 + q] = fmaxf(box[3 + q], sb[6 * (1 - slot) + 3 + q]);
+            box[q] = fminf(box[q], sib[q]);
+            box[3 + q] = fmaxf(box[3 + q], sib[3 + q]);
         }
         lo = plo;
         hi = phi;
@@ -465,17 +553,19 @@ cudaError_t launch_lbvh_build(const gray_params &p, cudaStream_t s) {
     const gray_scene &sc = p.scene;
     cudaError_t e;
     bounds_init_kernel<<<1, 32, 0, s>>>(sc.bounds);
-    bounds_kernel<<<blocks_for(n), kThreads, 0, s>>>(n, reinterpret_cast<const float4 *>(sc.aabb), sc.bounds);
+    bounds_kernel<<<min(blocks_for(n, kBoundsThreads), (unsigned)kBoundsMaxBlocks), kBoundsThreads, 0, s>>>(
+        n, reinterpret_cast<const float4 *>(sc.aabb), sc.bounds);
     morton_kernel<<<blocks_for(n), kThreads, 0, s>>>(n, reinterpret_cast<const float4 *>(sc.aabb), sc.bounds, sc.codes,
                                                     sc.order);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int tiles = (n + kSortTile - 1) / kSortTile;
     uint32_t *keys_alt = sc.sort_tmp, *vals_alt = sc.sort_tmp + n, *counts = sc.sort_tmp + 2 * (size_t)n;
+    uint32_t *totals = counts + 256 * (size_t)tiles;
     uint32_t *kin = sc.codes, *vin = sc.order, *kout = keys_alt, *vout = vals_alt;
     for (int shift = 0; shift < 32; shift += 8) {
         radix_hist_kernel<<<tiles, kSortThreads, 0, s>>>(n, shift, kin, counts, tiles);
-        radix_scan_kernel<<<1, 1024, 0, s>>>(counts, 256 * tiles);
-        radix_scatter_kernel<<<tiles, kSortThreads, 0, s>>>(n, shift, kin, vin, kout, vout, counts, tiles);
+        radix_row_scan_kernel<<<256, kScanThreads, 0, s>>>(counts, tiles, totals);
+        radix_scatter_kernel<<<tiles, kSortThreads, 0, s>>>(n, shift, kin, vin, kout, vout, counts, tiles, totals);
         uint32_t *tk = kin, *tv = vin;
         kin = kout;
         vin = vout;

@@ -58,7 +58,8 @@ class _Slot:
 
 class RenderServer:
     def __init__(self, tracers, slots: int = 2, max_batch: int = 32, reserve_bytes: int = 4 << 30,
-                 keep_images: bool = False, variant: int | None = None, blocks_per_sm: int | None = None):
+                 keep_images: bool = False, variant: int | None = None, blocks_per_sm: int | None = None,
+                 ray_budget: int | None = None):
         self.tracers = list(tracers)
         self.device = self.tracers[0].device
         self.slots = [_Slot(torch.cuda.Stream(self.device),
@@ -66,6 +67,10 @@ class RenderServer:
                                           variant=variant or DEFAULT_VARIANT,
                                           blocks_per_sm=blocks_per_sm or DEFAULT_BLOCKS_PER_SM, cache_plans=False)) for _ in range(slots)]
         self.max_batch = max_batch
+        # at most this many rays per batch (a batch always takes its first request): a batch's
+        # requests finish together, so an unbounded batch makes its small requests wait for its
+        # largest ones and holds its slot for long
+        self.ray_budget = ray_budget
         self.reserve = reserve_bytes
         self.keep_images = keep_images
         self.queue: list[Request] = []
@@ -114,7 +119,7 @@ class RenderServer:
                 sl.event, sl.batch, sl.bytes = None, [], 0
 
     def _admit(self, free_bytes: int):
-        batch, need = [], 0
+        batch, need, rays = [], 0, 0
         budget = free_bytes - self.reserve
         while self.queue and len(batch) < self.max_batch:
             r = self.queue[0]
@@ -123,8 +128,11 @@ class RenderServer:
                 break
             if not batch and b > budget:
                 break  # wait for memory to free up
+            if batch and self.ray_budget is not None and rays + r.rays > self.ray_budget:
+                break
             batch.append(self.queue.pop(0))
             need += b
+            rays += r.rays
         return batch, need
 
     def poll(self) -> int:

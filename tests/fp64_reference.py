@@ -71,3 +71,42 @@ def render(ray_o, ray_d, mean, rotation, log_scale, logit_opacity, channels, alp
         est = torch.where(sa_sum[:, None] > 0, sc / torch.clamp(sa_sum[:, None], min=1e-300), torch.zeros_like(sc))
         outs.append(C + (T_fin - full_T)[:, None] * est + bgt[None, :] * full_T[:, None])
     return torch.cat(outs, 0)
+
+
+SH_C0 = 0.28209479177387814
+
+
+def sh_colour(mean, cam_origin, sh_dc, sh_rest, degree):
+    """[N,3] SH colours in FP64, differentiable w.r.t. mean, sh_dc [N,1,3] and sh_rest [N,K,3].
+
+    Restates cuda/utils/sh.cu:11-78 and :224-247: the direction is the normalised mean - origin;
+    complex terms v(l, m), m = 0..l, from v(0,0) = C0, the diagonal v(l,l) = -sqrt((2l+1)/(2l)) (x+iy)
+    v(l-1,l-1), the sub-diagonal v(l,l-1) = sqrt(2l+1) z v(l-1,l-1) and the three-term recurrence
+    v(l,m) = a z v(l-1,m) + b v(l-2,m); per degree the basis is sqrt2 Im v(l,m) for m = l..1, Re v(l,0),
+    sqrt2 Re v(l,m) for m = 1..l; colour = max(C0 dc + sum basis * rest + 0.5, 0)."""
+    d = mean - cam_origin
+    d = d / torch.sqrt(torch.clamp((d * d).sum(-1, keepdim=True), min=1e-20))
+    x, y, z = d.unbind(-1)
+    vals = {(0, 0): (torch.full_like(x, SH_C0), torch.zeros_like(x))}
+    for l in range(1, degree + 1):
+        pr, pi = vals[(l - 1, l - 1)]
+        s = -math.sqrt((2 * l + 1) / (2 * l))
+        vals[(l, l)] = (s * (x * pr - y * pi), s * (x * pi + y * pr))
+        t = math.sqrt(2 * l + 1)
+        vals[(l, l - 1)] = (t * z * pr, t * z * pi)
+        for m in range(l - 2, -1, -1):
+            den = l * l - m * m
+            a = math.sqrt((4 * l * l - 1) / den)
+            b = -math.sqrt(((2 * l + 1) * ((l - 1) ** 2 - m * m)) / ((2 * l - 3) * den))
+            r1, i1 = vals[(l - 1, m)]
+            r2, i2 = vals[(l - 2, m)]
+            vals[(l, m)] = (a * z * r1 + b * r2, a * z * i1 + b * i2)
+    basis = []
+    for l in range(1, degree + 1):
+        basis += [math.sqrt(2.0) * vals[(l, m)][1] for m in range(l, 0, -1)]
+        basis.append(vals[(l, 0)][0])
+        basis += [math.sqrt(2.0) * vals[(l, m)][0] for m in range(1, l + 1)]
+    col = SH_C0 * sh_dc[:, 0, :] + 0.5
+    for k, bk in enumerate(basis):
+        col = col + bk[:, None] * sh_rest[:, k, :]
+    return torch.clamp(col, min=0.0)

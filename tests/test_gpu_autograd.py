@@ -129,3 +129,108 @@ def test_recompute_matches_stored(n, w, h):
     for a, b in zip(*grads):
         scale_ = b.abs().max().clamp(min=1e-12)
         assert ((a - b).abs().max() / scale_).item() < 1e-5
+
+
+def test_sh_gradients_vs_fp64_and_finite_differences():
+    """SH colours (degree 3) through RayTraceFunction: gradients w.r.t. sh_dc, sh_rest and mean (with
+    the view-direction term) against FP64 autograd of the reference's SH recurrence
+    (tests/fp64_reference.py sh_colour) and the compositing rule, and FP64 central differences
+    (h = 1e-6) on 200 random SH coefficients, where the loss is smooth (colour is linear in them), so
+    every one must agree."""
+    dev = torch.device("cuda")
+    sc = synthetic.gradcheck_scene(seed=0)
+    cam = synthetic.look_at((0.5, -7.0, 1.0), (0, 0, 0), (0, 0, 1), 0.75, 128, 128)
+    rt = classes.Raytracer(128, 128, sc.n, 3, 1, 8_000_000)
+    rt.get_config().t_threshold.fill_(0.03)
+    rt.get_config().zero_grads.fill_(False)
+    rt.get_gaussians().current_sh_degree.fill_(3)
+    mean, rot, scale, opac = [torch.from_numpy(a).to(dev).requires_grad_() for a in
+                              (sc.mean, sc.rotation, sc.scale, sc.opacity)]
+    dc = torch.from_numpy(sc.sh_dc).to(dev).requires_grad_()
+    rest = torch.from_numpy(sc.sh_rest).to(dev).requires_grad_()
+    g = rt.get_gaussians()
+    with torch.no_grad():
+        for dst, src in ((g.mean, mean), (g.rotation, rot), (g.scale, scale), (g.opacity, opac)):
+            dst.copy_(src)
+    rt.rebuild_bvh()
+    img = GA.render(rt, cam, mean, rot, scale, opac, sh_dc=dc, sh_rest=rest)
+    wgt = torch.from_numpy(np.random.default_rng(4).standard_normal((3, 128, 128))).to(dev)
+    (img.double() * wgt).sum().backward()
+    rt.check_status()
+    fb = rt.get_framebuffer()
+    ro = fb.ray_origin.reshape(-1, 3).double()
+    rd = fb.ray_direction.reshape(-1, 3).double()
+    origin = torch.from_numpy(np.asarray(cam.origin, np.float64)).to(dev)
+    p64 = [t.detach().double().requires_grad_() for t in (mean, rot, scale, opac, dc, rest)]
+
+    def loss64(ps):
+        col = F64.sh_colour(ps[0], origin, ps[4], ps[5], 3)
+        out = F64.render(ro, rd, ps[0], ps[1], ps[2], ps[3], col)
+        return (out.reshape(128, 128, 3).permute(2, 0, 1) * wgt).sum()
+
+    g64 = torch.autograd.grad(loss64(p64), p64)
+    for name, gg, ref in (("mean", mean.grad, g64[0]), ("sh_dc", dc.grad, g64[4]), ("sh_rest", rest.grad, g64[5])):
+        err = (gg.double() - ref).norm() / ref.norm()
+        assert err.item() < 1e-3, (name, err.item())
+    rng = np.random.default_rng(6)
+    flat = [t.detach().clone() for t in p64]
+    for _ in range(200):
+        k = 4 + int(rng.integers(0, 2))
+        idx = int(rng.integers(0, flat[k].numel()))
+        h = 1e-6
+        vals = []
+        for sgn in (1.0, -1.0):
+            ps = [t.clone() for t in flat]
+            ps[k].view(-1)[idx] += sgn * h
+            with torch.no_grad():
+                vals.append(float(loss64(ps)))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        gp = float((dc.grad if k == 4 else rest.grad).reshape(-1)[idx])
+        gmax = float(g64[k].abs().max())
+        assert abs(fd - gp) <= 1e-3 * gmax + 1e-3 * abs(fd), (k, idx, fd, gp)
+
+
+@pytest.mark.parametrize("recompute", [None, False, True])
+def test_renders_sharing_a_tracer_backpropagate_their_own_state(recompute, monkeypatch):
+    """Two views rendered on one tracer before one backward: the second forward evicts the first
+    render's state (copied out, or recomputed in its backward), so the gradients equal the sum of
+    the two views' gradients taken one at a time.  With recompute=None the copy is made only while it
+    fits in free memory; a huge reserve forces the recompute branch of that policy too."""
+    dev = torch.device("cuda")
+    n, w, h = 20_000, 160, 104
+    sc = synthetic.clustered_scene(n, seed=12)
+    cams = [synthetic.orbit_camera(0.9, w, h), synthetic.orbit_camera(2.4, w, h)]
+    rt = _tracer(sc.n, w, h, pool=16_000_000)
+    mean, rot, scale, opac, chan = _params(sc, dev)
+    g = rt.get_gaussians()
+    with torch.no_grad():
+        for dst, src in ((g.mean, mean), (g.rotation, rot), (g.scale, scale), (g.opacity, opac),
+                         (g.channels, chan)):
+            dst.copy_(src)
+    rt.rebuild_bvh()
+    gen = torch.Generator(device=dev).manual_seed(1)
+    wgts = [torch.randn(3, h, w, device=dev, generator=gen) for _ in cams]
+    params = (mean, rot, scale, opac, chan)
+
+    def grads_of(pairs, policy):
+        for t in params:
+            t.grad = None
+        loss = 0.0
+        for cam, wg in pairs:
+            loss = loss + (GA.render(rt, cam, *params[:4], channels=chan, recompute=policy) * wg).sum()
+        loss.backward()
+        return [t.grad.clone() for t in params]
+
+    single = [grads_of([(c, wg)], False) for c, wg in zip(cams, wgts)]
+    want = [a + b for a, b in zip(*single)]
+    if recompute is None:
+        for reserve in (GA._RESERVE_BYTES, 1 << 60):  # copy fits; copy never fits
+            monkeypatch.setattr(GA, "_RESERVE_BYTES", reserve)
+            got = grads_of(list(zip(cams, wgts)), None)
+            for a, b in zip(got, want):
+                assert ((a - b).abs().max() / b.abs().max().clamp(min=1e-12)).item() < 1e-5, reserve
+    else:
+        got = grads_of(list(zip(cams, wgts)), recompute)
+        for a, b in zip(got, want):
+            assert ((a - b).abs().max() / b.abs().max().clamp(min=1e-12)).item() < 1e-5
+    rt.check_status()

@@ -2,7 +2,9 @@
 forward outputs and hit lists on a seeded sample of pixels are bit-identical to the oracle's (own
 LBVH, same rays), the backward restricted to those pixels (upstream gradient zero elsewhere)
 matches the oracle's within the reduction-order tolerance, and a batched render of the view is
-bit-identical to the plain forward.  Needs a GB300 (about 5 GB of device memory)."""
+bit-identical to the plain forward.  The batching configuration's 16 uneven views, rendered in one
+batch, match the oracle on seeded pixels of every view.  Needs a GB300 (about 5 GB of device
+memory)."""
 import numpy as np
 import pytest
 import torch
@@ -109,3 +111,48 @@ def test_batched_view_equals_plain_at_full_size(scene):
         out = BatchRenderer([rt.cuda_module], use_graph=False, autotune=False).render([(0, cam)])[0]
     torch.cuda.synchronize()
     assert torch.equal(out, plain)
+
+
+def test_sixteen_uneven_views_in_one_batch_match_the_oracle(scene, oracle):
+    """The batching configuration: the benchmark's 16 views of uneven resolution (seed 0, as bench.py's
+    batched form) of the 3M scene rendered in one persistent launch; on 200 seeded pixels of every
+    view the batch's colour equals the oracle's bit for bit (the oracle traces the same rays through
+    its own LBVH with the view's SH colours)."""
+    sc, _, rt = scene
+    tr = rt.cuda_module
+    cams = synthetic.uneven_cameras(16, seed=0)
+    with torch.no_grad():
+        outs = BatchRenderer([tr], use_graph=False, autotune=False).render([(0, c) for c in cams])
+    torch.cuda.synchronize()
+    geom, l2w, aabb, vis = oracle.snapshot(sc.mean, sc.rotation, sc.scale, sc.opacity[:, 0])
+    live = oracle.forward_prep(sc.opacity[:, 0])
+    bvh = oracle.Bvh(aabb, vis)
+    cfg = oracle.TraceConfig(t_threshold=0.03)
+    rng = np.random.default_rng(11)
+    ro_all, rd_all, got_all, chans = [], [], [], []
+    for v, cam in enumerate(cams):
+        w, h = cam.image_width, cam.image_height
+        # the view's rays as the forward generates them (a training forward writes them out)
+        tr.set_render_resolution(w, h)
+        c = tr.get_camera()
+        c.znear.fill_(0.0)
+        c.zfar.fill_(99999.9)
+        c.vertical_fov_radians.fill_(float(cam.fov_y))
+        c.set_pose(cam.origin_cuda(), cam.rotation_c2w_blender_cuda())
+        tr.get_config().rays_from_python.fill_(False)
+        with torch.enable_grad():
+            tr.forward_pass()
+        fb = tr.get_framebuffer()
+        idx = rng.choice(w * h, 200, replace=False)
+        yy, xx = idx // w, idx % w
+        ro_all.append(fb.ray_origin[:h, :w].reshape(-1, 3)[torch.from_numpy(idx).cuda()].cpu().numpy())
+        rd_all.append(fb.ray_direction[:h, :w].reshape(-1, 3)[torch.from_numpy(idx).cuda()].cpu().numpy())
+        got_all.append(outs[v][:, yy, xx].T.cpu().numpy())
+        chans.append(oracle.sh_forward(3, sc.mean, np.asarray(cam.origin, np.float32), sc.sh_dc[:, 0, :],
+                                       sc.sh_rest))
+    tr.set_render_resolution(W, H)
+    torch.cuda.synchronize()
+    tr.check_status()
+    for v in range(len(cams)):
+        fwd = oracle.trace_forward(ro_all[v], rd_all[v], geom, live, chans[v], vis, cfg, bvh=bvh)
+        assert np.array_equal(got_all[v], fwd["rgb"]), v

@@ -16,9 +16,11 @@ def _cuda(gray_lib):
         pytest.skip("no CUDA device")
 
 
-def _scene_tracer(n, seed, maxw, maxh):
+def _scene_tracer(n, seed, maxw, maxh, sh_fp16=False):
+    """A resident inference scene: fp32 SH (the serving configuration's precision) or fp16 SH (the
+    reference's inference mode, cuda/core/gaussians.h:132)."""
     sc = synthetic.clustered_scene(n, seed=seed)
-    rt = classes.Raytracer(maxw, maxh, sc.n, 3, 1, 1, inference_only=True)
+    rt = classes.Raytracer(maxw, maxh, sc.n, 3, 1, 1, inference_only=True, inference_sh_fp16=sh_fp16)
     rt.get_config().t_threshold.fill_(0.03)
     g = rt.get_gaussians()
     with torch.no_grad():
@@ -30,8 +32,10 @@ def _scene_tracer(n, seed, maxw, maxh):
     return rt
 
 
-def test_served_results_equal_alone_and_in_mix():
-    tracers = [_scene_tracer(40_000, 1, 160, 120), _scene_tracer(90_000, 2, 160, 120)]
+@pytest.mark.parametrize("sh_fp16", [False, True])
+def test_served_results_equal_alone_and_in_mix(sh_fp16):
+    tracers = [_scene_tracer(40_000, 1, 160, 120, sh_fp16), _scene_tracer(90_000, 2, 160, 120, sh_fp16)]
+    assert tracers[0].get_gaussians().sh_coeffs_rest.dtype == (torch.float16 if sh_fp16 else torch.float32)
     rng = np.random.default_rng(0)
     res = [(64, 48), (160, 120), (96, 96)]
     sched = []

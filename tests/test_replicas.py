@@ -73,5 +73,10 @@ def test_reference_arm_json_line():
     assert d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 1 and d["higher_is_better"] is True
     assert d["config"]["workload"] == "train step, 64 uniform [-1,1]^3 Gaussians, 256x256"
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    # the line says that its steps were samples of the full step, how large, and what it spent
+    assert d["extrapolated"] is True and d["cpu_baseline"]["extrapolated"] is True
+    assert 0 < d["cpu_baseline"]["sampled_fraction"]["rays"] <= 1
+    assert d["timed_seconds"] > 0 and d["cpu_baseline"]["cpu"]
+    assert d["config"]["parallelism"] == "replicas x1"
     assert d["e2e"] == {"value": d["value"], "unit": "train-steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}

@@ -20,10 +20,11 @@ class _Tracer:
         return self._g
 
 
-def _server(max_batch=8, reserve=0, counts=(1000, 50_000)):
+def _server(max_batch=8, reserve=0, counts=(1000, 50_000), ray_budget=None):
     srv = object.__new__(serve.RenderServer)  # no CUDA streams: only the host-side admission is used
     srv.tracers = [_Tracer(n) for n in counts]
     srv.max_batch = max_batch
+    srv.ray_budget = ray_budget
     srv.reserve = reserve
     srv.queue = []
     srv._next = 0
@@ -69,3 +70,17 @@ def test_poisson_arrivals_are_seeded_and_increasing(rate):
     b = serve.poisson_arrivals(rate, 4000, seed=3)
     assert (a == b).all() and (a[1:] > a[:-1]).all()
     assert abs(a[-1] / 4000 - 1.0 / rate) < 0.1 / rate  # mean gap
+
+
+def test_ray_budget_bounds_a_batch_but_always_admits_one(gray_lib):
+    """With a ray budget, a batch takes requests in arrival order while their rays fit; a request
+    larger than the budget still goes, alone."""
+    srv = _server(max_batch=16, ray_budget=1920 * 1080 + 640 * 480)
+    for w, h in ((3840, 2160), (640, 480), (1920, 1080), (640, 480), (640, 480)):
+        srv.submit(0, _camera(w, h), arrival=0.0)
+    big, _ = srv._admit(1 << 40)
+    assert [r.camera.image_width for r in big] == [3840]
+    nxt, _ = srv._admit(1 << 40)
+    assert [r.camera.image_width for r in nxt] == [640, 1920]
+    rest, _ = srv._admit(1 << 40)
+    assert [r.camera.image_width for r in rest] == [640, 640]
