@@ -394,7 +394,7 @@ __device__ __forceinline__ void write_root_box(float *root_box, const float box[
 // node's index is one end of its range, so a local node's index is inside the block too).  The block
 // first loads the link / leaf-count words (node words 12-15) and the parents of the nodes indexed
 // base .. base + kThreads - 1 into shared memory, so the local climb makes no dependent global loads;
-// visit counters and the first arriver's box are in shared memory too, and the second arriver writes
+// visit counters and the children's boxes are in shared memory too, and the second arriver writes
 // the whole 64-byte node (both child boxes and the unchanged link words): full 32-byte sectors, no
 // partial-sector writes for the memory system to merge.  A climber tracks its subtree's leaf range
 // [lo, hi]; a parent reached through child 0 covers [lo, lo + leaves - 1], through child 1
@@ -412,7 +412,8 @@ __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const floa
                                                                uint32_t *__restrict__ queue, float *__restrict__ root_box,
                                                                int32_t *__restrict__ status) {
     __shared__ uint32_t sflag[kThreads];
-    __shared__ float sbox[kThreads][6];  // the first arriver's box at each local node
+    __shared__ float sbox[kThreads][12];  // the children's boxes at each local node, one slot per child
+                                          // (both may store before either counts its visit)
     __shared__ uint4 stopo[kThreads];    // node words 12-15 of the nodes base .. base + kThreads - 1
     __shared__ int32_t spar[kThreads];   // their parents
     const int base = blockIdx.x * kThreads;
@@ -460,13 +461,13 @@ __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const floa
         // p is local (its range lies inside the block, and p is one end of it)
         float *sb = sbox[p - base];
 #pragma unroll
-        for (int q = 0; q < 6; q++) sb[q] = box[q];
+        for (int q = 0; q < 6; q++) sb[6 * slot + q] = box[q];
         __threadfence_block();
         if (atomicAdd(&sflag[p - base], 1u) == 0u) return;
         __threadfence_block();
         float sib[6];
 #pragma unroll
-        for (int q = 0; q < 6; q++) sib[q] = sb[q];
+        for (int q = 0; q < 6; q++) sib[q] = sb[6 * (1 - slot) + q];
         const float *c0 = slot == 0 ? box : sib, *c1 = slot == 0 ? sib : box;
         float4 *nd = reinterpret_cast<float4 *>(nodes) + 4 * (size_t)p;
         __stcg(nd, make_float4(c0[0], c0[1], c0[2], c0[3]));

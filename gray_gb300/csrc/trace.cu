@@ -49,6 +49,7 @@ constexpr int kFrontierMax = kFrontierWords - 1;
 constexpr int kFrontierSort = 256;  // sort buffer of the frontier walk (a power of two > kFrontierMax)
 constexpr uint32_t kFrontierNone = 0xFFFFFFFFu;
 constexpr int kFrontierCutDefault = 64;  // frontier nodes hold at most this many leaves
+constexpr int kTilesPerClaim = 8;        // tiles a block of the scheduled forward claims at a time
 
 struct FwdArgs {
     uint32_t alloc_w, render_w, render_h;
@@ -416,8 +417,9 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
 // One full traversal of the packet (camera rays with a common origin) with the node work spread
 // over the lanes: each step pops up to 32 nodes, one per lane, tests their child boxes against the
 // packet frustum, pushes surviving internal children and queues surviving leaves; queued leaves
-// are then intersected by every lane with its own ray (on_leaf).  With a tile frontier (front =
-// count, entries; a count of kFrontierNone or a null front: none) the traversal starts there instead
+// are then intersected by every lane with its own ray (on_leaf).  With a tile frontier (at
+// front_base + front_off: count, entries; a count of kFrontierNone or a null base: none; base and
+// offset are kept apart so that a kernel-parameter base needs no register) the traversal starts there instead
 // of at the root: the frontier goes onto the stack with its first entry on top, and a frontier leaf
 // is queued when it is popped.  Returns false if the shared stack overflowed (the caller then
 // repeats the traversal per ray).
@@ -425,7 +427,8 @@ template <int KB, bool LO>
 __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool want,
                                                  bool first, LaneState &st, unsigned long long (*kbuf)[kFwdThreads],
                                                  const Frustum &fr, uint32_t *stk, uint32_t *cand,
-                                                 CandCache &cc, const uint32_t *front, int32_t *status) {
+                                                 CandCache &cc, const uint32_t *front_base, uint32_t front_off,
+                                                 int32_t *status) {
     const int lane = threadIdx.x & 31;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     const int n = sc.n;
@@ -436,6 +439,7 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
         on_leaf<KB>(sc, 0u, want, first, ro, rd, k, st, kbuf);
         return true;
     }
+    const uint32_t *front = front_base ? front_base + front_off : nullptr;
     int sp = front ? (int)front[0] : -1, nc = 0;
     if (sp >= 0 && sp <= kFrontierMax) {
         for (int i = lane; i < sp; i += 32) stk[sp - 1 - i] = front[1 + i];
@@ -540,7 +544,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
                                           unsigned long long (*kbuf)[kFwdThreads], RayResult &res,
                                           const Frustum *fr = nullptr, uint32_t *wstk = nullptr,
                                           uint32_t *wcand = nullptr, CandCache *wcc = nullptr,
-                                          const uint32_t *front = nullptr) {
+                                          const uint32_t *front_base = nullptr, uint32_t front_off = 0) {
     const int lane = threadIdx.x & 31;
     LaneState &st = res.st;
     st.lfx = 0;
@@ -567,7 +571,8 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
         // ---------------- traversal ----------------
         bool per_ray = fr == nullptr;
         if (!per_ray &&
-            !traverse_frustum<KB, LO>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, *wcc, front, status)) {
+            !traverse_frustum<KB, LO>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, *wcc, front_base, front_off,
+                                      status)) {
             // the frustum traversal gave up (stack overflow): discard what it gathered, trace per ray
             st.kcount = 0;
             st.ncand = 0;
@@ -815,14 +820,16 @@ struct FwdShared {
     uint32_t front[kFrontierWords];  // the tile's BVH frontier (count, entries)
 };
 
-// One block's pixel tile (bx, by): 2x2 packets of tile_w x tile_h pixels, one per warp.
+// Packet (wx, wy) of pixel tile (bx, by) (a tile is 2x2 packets of tile_w x tile_h pixels), traced
+// by the calling warp; front_base + front_off: the tile's BVH frontier (count, entries), or a null base.
 template <int KB, bool LO>
-__device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, FwdShared<KB> &sh) {
+__device__ __forceinline__ void forward_packet(const FwdArgs &a, int bx, int by, int wx, int wy,
+                                               const uint32_t *front_base, uint32_t front_off, FwdShared<KB> &sh) {
     unsigned long long(*kbuf)[kFwdThreads] = sh.kbuf;
     Frustum *sfr = sh.sfr;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int px = bx * (a.tile_w * kBlockWarpsX) + (warp % kBlockWarpsX) * a.tile_w + (lane % a.tile_w);
-    const int py = by * (a.tile_h * kBlockWarpsY) + (warp / kBlockWarpsX) * a.tile_h + (lane / a.tile_w);
+    const int px = bx * (a.tile_w * kBlockWarpsX) + wx * a.tile_w + (lane % a.tile_w);
+    const int py = by * (a.tile_h * kBlockWarpsY) + wy * a.tile_h + (lane / a.tile_w);
     const bool inside = px < (int)a.render_w && py < (int)a.render_h;
     const uint32_t pixel = (uint32_t)py * a.alloc_w + (uint32_t)px;
 
@@ -864,16 +871,6 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
 
     // camera rays of the packet share the origin: trace with the frustum traversal
     const bool frustum = !*a.rays_from_python && !*a.jitter;
-    // the tile's frontier, read once by the block (every thread of the block gets here together)
-    {
-        const uint32_t *src = a.frontier ? a.frontier + (size_t)(by * a.tiles_x + bx) * kFrontierWords : nullptr;
-        const uint32_t cnt = src && frustum ? src[0] : kFrontierNone;
-        const bool use = cnt <= (uint32_t)kFrontierMax;
-        if (use)
-            for (uint32_t i = threadIdx.x; i < cnt; i += kFwdThreads) sh.front[1 + i] = src[1 + i];
-        if (threadIdx.x == 0) sh.front[0] = use ? cnt : kFrontierNone;
-        __syncthreads();
-    }
     if (frustum) {
         const int x0 = px - lane % a.tile_w, y0 = py - lane / a.tile_w;
         const int x1 = x0 + a.tile_w - 1, y1 = y0 + a.tile_h - 1;
@@ -882,7 +879,7 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
     }
     RayResult r;
     trace_ray<KB, LO>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sh.sstk[warp],
-                  sh.scand[warp], &sh.scc[warp], sh.front);
+                  sh.scand[warp], &sh.scc[warp], frustum ? front_base : nullptr, front_off);
 
     if (!inside) return;
     if (!alive) {
@@ -922,6 +919,23 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
     }
 }
 
+// One block's pixel tile (bx, by): its four packets, one per warp; the tile's frontier is copied
+// into shared memory once by the block.
+template <int KB, bool LO>
+__device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, FwdShared<KB> &sh) {
+    const int warp = threadIdx.x >> 5;
+    {   // every thread of the block gets here together
+        const uint32_t *src = a.frontier ? a.frontier + (size_t)(by * a.tiles_x + bx) * kFrontierWords : nullptr;
+        const uint32_t cnt = src ? src[0] : kFrontierNone;
+        const bool use = cnt <= (uint32_t)kFrontierMax;
+        if (use)
+            for (uint32_t i = threadIdx.x; i < cnt; i += kFwdThreads) sh.front[1 + i] = src[1 + i];
+        if (threadIdx.x == 0) sh.front[0] = use ? cnt : kFrontierNone;
+        __syncthreads();
+    }
+    forward_packet<KB, LO>(a, bx, by, warp % kBlockWarpsX, warp / kBlockWarpsX, sh.front, 0u, sh);
+}
+
 // Grid launch: block (x, y) renders tile (x, y).
 template <int KB, int MINB>
 __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const FwdArgs a) {
@@ -945,6 +959,43 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_sched_kernel(
         if (t >= (uint32_t)a.ntiles) break;
         const uint32_t tile = a.schedule[kSchedHeader + a.ntiles + t];
         forward_tile<KB, (MINB < 6)>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x), sh);
+    }
+}
+
+// Persistent launch with packets taken per warp: a block claims kTilesPerClaim tiles at a time from
+// the schedule's order, densest first, and its warps take the claimed tiles' packets from a counter
+// in shared memory (a tile's four packets in turn, so they run side by side on the SM and share its
+// L1): a warp whose packet finishes early starts the next one instead of waiting at a block barrier
+// for the tile's slowest packet; the block meets a barrier once per claim.  Packets read their
+// tile's frontier from the schedule buffer (L2).  The loop state lives in shared memory and the
+// kernel parameters, not in registers that would stay live across a packet's trace.
+template <int KB, int MINB>
+__global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_claim_kernel(const FwdArgs a) {
+    __shared__ FwdShared<KB> sh;
+    __shared__ uint32_t s_base, s_packets, s_packet;
+    if (*a.render_ellipsoids) return;
+    for (;;) {
+        __syncthreads();  // every warp is done with the previous claim (s_base, s_packet)
+        if (threadIdx.x == 0) {
+            const uint32_t base = atomicAdd(a.schedule, (uint32_t)kTilesPerClaim);
+            s_base = base;
+            s_packets = base < (uint32_t)a.ntiles ? (uint32_t)kWarps * min((uint32_t)kTilesPerClaim,
+                                                                             (uint32_t)a.ntiles - base)
+                                                  : 0u;
+            s_packet = 0u;
+        }
+        __syncthreads();
+        if (s_packets == 0u) break;
+        for (;;) {
+            uint32_t q = 0u;
+            if ((threadIdx.x & 31) == 0) q = atomicAdd(&s_packet, 1u);
+            q = __shfl_sync(kFull, q, 0);
+            if (q >= s_packets) break;
+            const uint32_t tile = a.schedule[kSchedHeader + a.ntiles + s_base + q / kWarps], sub = q % kWarps;
+            forward_packet<KB, (MINB < 6)>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x),
+                                           (int)(sub % kBlockWarpsX), (int)(sub / kBlockWarpsX), a.frontier,
+                                           tile * (uint32_t)kFrontierWords, sh);
+        }
     }
 }
 
@@ -1434,14 +1485,18 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
                               vw.height, s_sc[warp].root_box);
         }
         const uint32_t *front = nullptr;
+        uint32_t front_off = 0u;
         if (frontier) {
             const uint32_t tx = local % tiles_x, ty = local / tiles_x;
             const uint32_t grp = vw.group_offset + (ty / 2) * ((tiles_x + 1) / 2) + tx / 2;
-            if (grp < total_groups) front = frontier + (size_t)grp * kFrontierWords;  // else: from the root
+            if (grp < total_groups) {  // else: from the root
+                front = frontier;
+                front_off = grp * (uint32_t)kFrontierWords;
+            }
         }
         RayResult r;
         trace_ray<KB, (MINB < 6)>(sc, k, ro, rd, inside, false, hs, status, kbuf, r, &sfr[warp], sstk[warp], scand[warp],
-                      &scc[warp], front);
+                      &scc[warp], front, front_off);
         if (!inside) continue;
         float r0, r1, r2;
         finish_ray(r, bs.bg, 1e-12f, false, r0, r1, r2);
@@ -1522,9 +1577,11 @@ cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s
 cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_t s) {
     FwdArgs a = forward_args(p, display);
     // variant: bits 0-1 select (buffer size, register cap), bit 2 the packet shape, bits 3-4 the
-    // tile frontier's cut (64 leaves, 32, 128, no frontier)
+    // tile frontier's cut (64 leaves, 32, 128, no frontier), bit 5 packets taken per warp from
+    // claimed groups of tiles (trace_forward_claim_kernel) instead of one tile per block
     const int v = p.trace_variant > 0 ? p.trace_variant : kDefaultTraceVariant;
     const int fcut = (v >> 3) & 3;
+    const bool claim = (v & 32) != 0;
     a.tile_w = (v & 4) ? 4 : 8;
     a.tile_h = 32 / a.tile_w;
     const int bw = a.tile_w * kBlockWarpsX, bh = a.tile_h * kBlockWarpsY;
@@ -1535,16 +1592,17 @@ cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_
     const void *kern;
     const size_t words = gray_schedule_words_for(p.image_width, p.image_height);
     const bool sched = p.hitlist.schedule && a.ntiles > 0 && (size_t)a.ntiles <= (words - kSchedHeader) / 2;
+#define GRAY_FWD_KERNEL(KB, MINB)                                                                   \
+    (!sched ? reinterpret_cast<const void *>(&trace_forward_kernel<KB, MINB>)                       \
+     : claim ? reinterpret_cast<const void *>(&trace_forward_claim_kernel<KB, MINB>)                \
+             : reinterpret_cast<const void *>(&trace_forward_sched_kernel<KB, MINB>))
     switch (v & 3) {
-        case 0: kern = sched ? reinterpret_cast<const void *>(&trace_forward_sched_kernel<32, 1>)
-                             : reinterpret_cast<const void *>(&trace_forward_kernel<32, 1>); break;
-        case 1: kern = sched ? reinterpret_cast<const void *>(&trace_forward_sched_kernel<32, 4>)
-                             : reinterpret_cast<const void *>(&trace_forward_kernel<32, 4>); break;
-        case 2: kern = sched ? reinterpret_cast<const void *>(&trace_forward_sched_kernel<16, 1>)
-                             : reinterpret_cast<const void *>(&trace_forward_kernel<16, 1>); break;
-        default: kern = sched ? reinterpret_cast<const void *>(&trace_forward_sched_kernel<16, 6>)
-                              : reinterpret_cast<const void *>(&trace_forward_kernel<16, 6>); break;
+        case 0: kern = GRAY_FWD_KERNEL(32, 1); break;
+        case 1: kern = GRAY_FWD_KERNEL(32, 4); break;
+        case 2: kern = GRAY_FWD_KERNEL(16, 1); break;
+        default: kern = GRAY_FWD_KERNEL(16, 6); break;
     }
+#undef GRAY_FWD_KERNEL
     cudaError_t e;
     if (sched) {
         // densest tiles first: estimate, bucket, then a persistent grid that takes tiles in order
