@@ -2,12 +2,13 @@
 that the ray tracing path, its optimiser and its training cadence read, under the reference's
 field names and defaults so that a reference config drops in.  Training-loop product features
 (logging, previews, LR schedules, SSIM, half-resolution warm-up) are not on the path and have no
-field here; the MLP and exposure-compensation switches are kept only so that a config asking for
-them is refused (gray_gb300.Raytracer raises NotImplementedError)."""
+field here.  The post-processing MLP's knobs are kept (gray_gb300.mlp.PostMLP); the pre-MLP and
+exposure-compensation switches are kept only so that a config asking for them is refused
+(gray_gb300.Raytracer raises NotImplementedError)."""
 from __future__ import annotations
 
 from dataclasses import dataclass, field
-from typing import List
+from typing import List, Optional
 
 
 @dataclass
@@ -56,10 +57,16 @@ class RaytracerConfig:
     sh_max_degree: int = 3
     sh_increment_interval: int = 1000
 
+    # post-processing MLP on the ray / depth outputs (gray_gb300.mlp.PostMLP)
+    post_mlp: bool = False
+    post_mlp_width: int = 128
+    post_mlp_layers: int = 5
+    post_mlp_lr: float = 1e-3
+    post_mlp_freq_bands: Optional[int] = 1
+
     # not on the path: refused when set
     exposure_comp_enabled: bool = False
     pre_mlp: bool = False
-    post_mlp: bool = False
 
     def __post_init__(self):
         if not 0 <= self.sh_max_degree <= 3:

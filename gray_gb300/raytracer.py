@@ -3,8 +3,9 @@
 Same constructor, __call__ / backward / step / set_render_resolution / prune /
 update_pruning_stats / from_point_cloud / from_safetensors / save_safetensors, and the same
 `cuda_module` attribute, which here is gray_gb300.classes.Raytracer instead of
-torch.classes.gray.Raytracer.  The pre-/post-processing MLPs and exposure compensation of the
-reference are outside the ray tracing path and not provided (their flags must stay False).
+torch.classes.gray.Raytracer.  The post-processing MLP (the consumer of the ray and depth outputs)
+is gray_gb300.mlp.PostMLP; the pre-processing MLP and exposure compensation of the reference are
+outside the ray tracing path and not provided (their flags must stay False).
 """
 from __future__ import annotations
 
@@ -23,8 +24,8 @@ class Raytracer(torch.nn.Module):
     def __init__(self, cfg: RaytracerConfig, num_points: int, image_width: int, image_height: int,
                  inference_only: bool = False):
         super().__init__()
-        if cfg.pre_mlp or cfg.post_mlp or cfg.exposure_comp_enabled:
-            raise NotImplementedError("pre/post MLPs and exposure compensation are not part of gray_gb300")
+        if cfg.pre_mlp or cfg.exposure_comp_enabled:
+            raise NotImplementedError("the pre-MLP and exposure compensation are not part of gray_gb300")
         self.cfg = cfg
         self.image_width = image_width
         self.image_height = image_height
@@ -54,6 +55,14 @@ class Raytracer(torch.nn.Module):
         g.beta_2.fill_(cfg.beta_2)
         g.epsilon.fill_(cfg.epsilon)
         g.sh_update_laziness.fill_(cfg.sh_update_laziness)
+        num_channels = self.cuda_module.get_num_channels()
+        if num_channels != 3 and not cfg.post_mlp:
+            raise ValueError("the post-processing MLP must be enabled when the tracer has other than 3 channels")
+        self.post_mlp = None
+        if cfg.post_mlp:
+            from .mlp import PostMLP
+
+            self.post_mlp = PostMLP(cfg, num_channels)
         self.output_channels = None
 
     def __call__(self, cam_info: CameraInfo, znear=0.0, zfar=99999.9, skip_copy=False):
@@ -77,6 +86,12 @@ class Raytracer(torch.nn.Module):
             assert self.output_channels is None, "Called the forward pass multiple times without a backward pass"
             out.requires_grad_()
             self.output_channels = out
+        if self.post_mlp is not None:
+            # gray/raytracer.py:163-167: hit points from the depth along each ray
+            ray_direction = framebuffer.ray_direction.detach()[:h, :w].moveaxis(-1, 0)
+            depth = framebuffer.output_depth.detach()[:h, :w].moveaxis(-1, 0)
+            hit_point = cam_info.origin_cuda()[:, None, None] + depth * ray_direction
+            return self.post_mlp(out, hit_point, ray_direction)
         return out
 
     def backward(self, loss):
@@ -92,6 +107,8 @@ class Raytracer(torch.nn.Module):
         self.update_pruning_stats()
         self.cuda_module.step()
         self.cuda_module.update_bvh()
+        if self.post_mlp is not None:
+            self.post_mlp.step()
 
     def set_render_resolution(self, width: int, height: int):
         self.render_width = width
