@@ -409,8 +409,9 @@ def gpu_arm(a, rank, world, local_rank):
     peak, peak_kind = measured_peak_gbs()
     achieved = algo.get(dominant, 0.0) / (dom_ms / 1000.0) / 1e9
     # kernels behind one profiled scope: adam = step count + update; trace_backward = backward
-    # record + replay; trace_forward = tile work estimate + bucket scan + scatter + trace
-    kernels_per_group = {"adam": 2, "trace_backward": 2, "trace_forward": 4}
+    # record + replay; trace_forward = tile work estimate + bucket scan + scatter + trace; refit =
+    # block-local climb + upper tree
+    kernels_per_group = {"adam": 2, "trace_backward": 2, "trace_forward": 4, "refit": 2}
     launches = sum(cnt * kernels_per_group.get(name, 1) for name, (_, cnt) in res.items())
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,

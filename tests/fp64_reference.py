@@ -26,8 +26,12 @@ def quat_to_rot(q):
 
 
 def render(ray_o, ray_d, mean, rotation, log_scale, logit_opacity, channels, alpha_threshold=0.01, t_threshold=0.03,
-           bg=(0.0, 0.0, 0.0), chunk=4096):
-    """ray_o, ray_d: [R,3]; returns [R,3] colours (float64, differentiable w.r.t. the parameters)."""
+           bg=(0.0, 0.0, 0.0), chunk=4096, tail_channels=None):
+    """ray_o, ray_d: [R,3]; returns [R,3] colours (float64, differentiable w.r.t. the parameters).
+
+    tail_channels: colours for the truncated-tail estimate (default: channels).  The reference's
+    backward treats that estimate as a constant (it replays composited hits only), so a finite
+    difference of a colour parameter matches its gradient only with the tail's colours held fixed."""
     o = torch.sigmoid(logit_opacity.reshape(-1))
     sf = torch.where(o > alpha_threshold, (4.0 * torch.log(torch.clamp(o / alpha_threshold, min=1.0))) ** 0.25,
                      torch.zeros_like(o)).detach()
@@ -56,6 +60,7 @@ def render(ray_o, ray_d, mean, rotation, log_scale, logit_opacity, channels, alp
         selectable = torch.gather(hit & (t16 > 0), 1, order)
         a_s = torch.gather(alpha, 1, order)
         c_s = channels[order]                                        # [r,N,3]
+        ct_s = c_s if tail_channels is None else tail_channels[order]
         one_minus = 1.0 - a_s
         T_after = torch.cumprod(torch.where(selectable, one_minus, torch.ones_like(one_minus)), dim=-1)
         T_before = torch.cat([torch.ones_like(T_after[:, :1]), T_after[:, :-1]], dim=-1)
@@ -66,7 +71,7 @@ def render(ray_o, ray_d, mean, rotation, log_scale, logit_opacity, channels, alp
         full_T = torch.prod(one_minus, dim=-1)
         skipped = (~comp) & (a_s.detach() > 0)
         sa = torch.where(skipped, a_s, torch.zeros_like(a_s)).detach()
-        sc = (sa[..., None] * c_s).sum(1).detach()
+        sc = (sa[..., None] * ct_s).sum(1).detach()
         sa_sum = sa.sum(-1)
         est = torch.where(sa_sum[:, None] > 0, sc / torch.clamp(sa_sum[:, None], min=1e-300), torch.zeros_like(sc))
         outs.append(C + (T_fin - full_T)[:, None] * est + bgt[None, :] * full_T[:, None])
