@@ -49,7 +49,6 @@ constexpr int kFrontierMax = kFrontierWords - 1;
 constexpr int kFrontierSort = 256;  // sort buffer of the frontier walk (a power of two > kFrontierMax)
 constexpr uint32_t kFrontierNone = 0xFFFFFFFFu;
 constexpr int kFrontierCutDefault = 64;  // frontier nodes hold at most this many leaves
-constexpr int kTilesPerClaim = 8;        // tiles a block of the scheduled forward claims at a time
 
 struct FwdArgs {
     uint32_t alloc_w, render_w, render_h;
@@ -962,40 +961,24 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_sched_kernel(
     }
 }
 
-// Persistent launch with packets taken per warp: a block claims kTilesPerClaim tiles at a time from
-// the schedule's order, densest first, and its warps take the claimed tiles' packets from a counter
-// in shared memory (a tile's four packets in turn, so they run side by side on the SM and share its
-// L1): a warp whose packet finishes early starts the next one instead of waiting at a block barrier
-// for the tile's slowest packet; the block meets a barrier once per claim.  Packets read their
-// tile's frontier from the schedule buffer (L2).  The loop state lives in shared memory and the
-// kernel parameters, not in registers that would stay live across a packet's trace.
+// Persistent launch with packets taken per warp: every warp claims the next packet (a quarter of a
+// pixel tile, tiles in the schedule's densest-first order) from the global counter on its own, so no
+// warp waits at a block barrier for a tile's slowest packet; a tile's four packets usually land on
+// different SMs, though, so they no longer share an L1.  Packets read their tile's frontier from
+// the schedule buffer (L2).
 template <int KB, int MINB>
 __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_claim_kernel(const FwdArgs a) {
     __shared__ FwdShared<KB> sh;
-    __shared__ uint32_t s_base, s_packets, s_packet;
     if (*a.render_ellipsoids) return;
     for (;;) {
-        __syncthreads();  // every warp is done with the previous claim (s_base, s_packet)
-        if (threadIdx.x == 0) {
-            const uint32_t base = atomicAdd(a.schedule, (uint32_t)kTilesPerClaim);
-            s_base = base;
-            s_packets = base < (uint32_t)a.ntiles ? (uint32_t)kWarps * min((uint32_t)kTilesPerClaim,
-                                                                             (uint32_t)a.ntiles - base)
-                                                  : 0u;
-            s_packet = 0u;
-        }
-        __syncthreads();
-        if (s_packets == 0u) break;
-        for (;;) {
-            uint32_t q = 0u;
-            if ((threadIdx.x & 31) == 0) q = atomicAdd(&s_packet, 1u);
-            q = __shfl_sync(kFull, q, 0);
-            if (q >= s_packets) break;
-            const uint32_t tile = a.schedule[kSchedHeader + a.ntiles + s_base + q / kWarps], sub = q % kWarps;
-            forward_packet<KB, (MINB < 6)>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x),
-                                           (int)(sub % kBlockWarpsX), (int)(sub / kBlockWarpsX), a.frontier,
-                                           tile * (uint32_t)kFrontierWords, sh);
-        }
+        uint32_t q = 0u;
+        if ((threadIdx.x & 31) == 0) q = atomicAdd(a.schedule, 1u);
+        q = __shfl_sync(kFull, q, 0);
+        if (q >= (uint32_t)kWarps * (uint32_t)a.ntiles) break;
+        const uint32_t tile = a.schedule[kSchedHeader + a.ntiles + q / kWarps], sub = q % kWarps;
+        forward_packet<KB, (MINB < 6)>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x),
+                                       (int)(sub % kBlockWarpsX), (int)(sub / kBlockWarpsX), a.frontier,
+                                       tile * (uint32_t)kFrontierWords, sh);
     }
 }
 
@@ -1577,8 +1560,8 @@ cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s
 cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_t s) {
     FwdArgs a = forward_args(p, display);
     // variant: bits 0-1 select (buffer size, register cap), bit 2 the packet shape, bits 3-4 the
-    // tile frontier's cut (64 leaves, 32, 128, no frontier), bit 5 packets taken per warp from
-    // claimed groups of tiles (trace_forward_claim_kernel) instead of one tile per block
+    // tile frontier's cut (64 leaves, 32, 128, no frontier), bit 5 packets claimed per warp
+    // (trace_forward_claim_kernel) instead of tiles per block
     const int v = p.trace_variant > 0 ? p.trace_variant : kDefaultTraceVariant;
     const int fcut = (v >> 3) & 3;
     const bool claim = (v & 32) != 0;

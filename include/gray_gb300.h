@@ -169,7 +169,7 @@ typedef struct gray_params {
      * 32 or 16 keys and register cap, bit 2 = 8x4 or 4x8 pixel packets, bits 3-4 = where a pixel
      * tile's traversals start (BVH nodes of at most 64, 32 or 128 leaves that the tile's frustum
      * reaches, or the root), bit 5 = how the scheduled launch hands out work (one pixel tile per
-     * block, or groups of tiles per block whose packets the block's warps take one at a time).
+     * block, or one packet per warp).
      * Results are identical for every variant; only speed differs. */
     int32_t trace_variant;
 } gray_params;

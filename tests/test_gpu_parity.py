@@ -363,8 +363,8 @@ def test_clustered_scene_with_bvh(oracle):
 @pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 15, 23, 31, 8 + 3, 32 + 7, 32 + 1, 32 + 4, 32 + 31])
 def test_trace_variants_are_bit_identical(oracle, variant):
     """Every forward-kernel variant (hit buffer size, register cap, packet shape, tile frontier cut
-    of 64, 32 or 128 leaves or none, one tile per block or packets taken per warp from claimed
-    groups of tiles) gives the same bits as the oracle: the variant only changes
+    of 64, 32 or 128 leaves or none, one tile per block or one packet per warp) gives the same bits
+    as the oracle: the variant only changes
     speed."""
     sc = synthetic.clustered_scene(40_000, seed=8)
     chan = np.random.default_rng(2).uniform(0, 1, (sc.n, 3)).astype(np.float32)
