@@ -55,9 +55,10 @@ def parse_args(argv):
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--no-served", action="store_true", help="skip the served measurement only")
     ap.add_argument("--trace-variant", type=int, default=0, help="forward-kernel variant (0 = library default)")
-    ap.add_argument("--record-traffic", nargs="+", metavar=("CSV", "KEY"),
-                    help="store the DRAM bytes of an ncu CSV capture (CSV KEY [UNITS_SCALE]) in "
-                         "profiles/ncu_traffic.json with the digest of the current kernel sources, and exit")
+    ap.add_argument("--record-traffic", nargs="+", metavar="ARG",
+                    help="CSV KEY KERNEL [UNITS_SCALE]: store the per-launch DRAM bytes of KERNEL in an ncu CSV "
+                         "capture under KEY in profiles/ncu_traffic.json, with the digest of the current kernel "
+                         "sources, and exit")
     ap.add_argument("--scene", default="clustered", choices=["clustered", "small", "gradcheck"],
                     help="clustered: --n-gaussians clustered Gaussians on a radius-8 orbit; small: 64 Gaussians in "
                          "[-1,1]^3, 256x256 camera at distance 4 (fx = 256); gradcheck: 1000 Gaussians in [-2,2]^3, "
@@ -236,11 +237,11 @@ def ncu_traffic(kernel, a):
     return entry.get("bytes")
 
 
-def record_traffic(csv_path, key, per_launch_units=1.0):
-    """Add the DRAM bytes of the kernel launches in an ncu CSV (--metrics dram__bytes_read.sum,
-    dram__bytes_write.sum --csv) to profiles/ncu_traffic.json under `key`, averaged per launch and
-    scaled by per_launch_units (a capture of a smaller case scaled to the full launch), together with
-    the digest of the kernel sources it was captured on."""
+def record_traffic(csv_path, key, kernel, per_launch_units=1.0):
+    """Add the DRAM bytes of the launches of `kernel` (a substring of the kernel name) in an ncu CSV
+    (--metrics dram__bytes_read.sum,dram__bytes_write.sum --csv) to profiles/ncu_traffic.json under
+    `key`, averaged per launch and scaled by per_launch_units (a capture of a smaller case scaled to
+    the full launch), together with the digest of the kernel sources it was captured on."""
     import csv
 
     per_launch = {}
@@ -248,10 +249,10 @@ def record_traffic(csv_path, key, per_launch_units=1.0):
         rows = [r for r in csv.reader(f) if r]
     head = next(i for i, r in enumerate(rows) if "Metric Name" in r)
     cols = rows[head]
-    mi, vi, ii = cols.index("Metric Name"), cols.index("Metric Value"), cols.index("ID")
+    mi, vi, ii, ki = cols.index("Metric Name"), cols.index("Metric Value"), cols.index("ID"), cols.index("Kernel Name")
     units = rows[head + 1] if rows[head + 1][mi] == "" else None
     for r in rows[head + 1 + (1 if units else 0):]:
-        if r[mi] in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+        if kernel in r[ki] and r[mi] in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
             v = float(r[vi].replace(",", ""))
             unit = r[cols.index("Metric Unit")] if "Metric Unit" in cols else "byte"
             v *= {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "KB": 1e3, "MB": 1e6, "GB": 1e9}.get(unit, 1)
@@ -261,7 +262,9 @@ def record_traffic(csv_path, key, per_launch_units=1.0):
         table = json.load(open(TRAFFIC_FILE))
     except Exception:
         table = {}
-    table[key] = {"bytes": int(avg), "launches": len(per_launch), "sources": kernel_source_hash()}
+    if not per_launch:
+        raise ValueError(f"no launch of a kernel named like {kernel!r} in {csv_path}")
+    table[key] = {"bytes": int(avg), "launches": len(per_launch), "kernel": kernel, "sources": kernel_source_hash()}
     json.dump(table, open(TRAFFIC_FILE, "w"), indent=1, sort_keys=True)
     return table[key]
 
@@ -432,7 +435,7 @@ def gpu_arm(a, rank, world, local_rank):
 
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
-        cpu = cpu_baseline(a, sc, cam)
+        cpu = cpu_baseline(a)
 
     line = {"metric": METRIC, "value": round(steps_per_s, 3), "unit": "train-steps/s", "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
@@ -712,12 +715,21 @@ class CpuScene:
 CPU_BASELINE_STEPS, CPU_BASELINE_WARMUP = 3, 1
 
 
-def cpu_baseline(a, sc, cam):
-    cs = CpuScene(a, sc, cam)
-    t, spent, fwd = cs.measure(CPU_BASELINE_STEPS, CPU_BASELINE_WARMUP)
-    out = {"value": round(1.0 / t, 5), "unit": "train-steps/s"}
-    out.update(cs.describe(CPU_BASELINE_STEPS, spent))
-    out["hits_per_ray_sample"] = round(float(fwd["nhit"].mean()), 2)
+def cpu_baseline(a):
+    """The reference arm's measurement (--impl reference) on this workload, run in a process of its own:
+    inside the GPU arm's process the CUDA context and torch's worker threads share the host cores
+    with the oracle's threads and slowed it by half; a separate process measures the same thing the
+    reference arm does."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--steps", str(CPU_BASELINE_STEPS),
+           "--warmup", str(CPU_BASELINE_WARMUP), "--scene", a.scene, "--n-gaussians", str(a.n_gaussians),
+           "--width", str(a.width), "--height", str(a.height), "--cpu-sample-stride", str(a.cpu_sample_stride)]
+    env = dict(os.environ, WORLD_SIZE="1", RANK="0", LOCAL_RANK="0", CUDA_VISIBLE_DEVICES="")
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=1800)
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    if r.returncode != 0 or not lines:
+        return {"value": None, "error": (r.stderr or r.stdout)[-300:]}
+    out = json.loads(lines[-1])["cpu_baseline"]
+    out["process"] = "separate (bench.py --impl reference)"
     return out
 
 
@@ -731,10 +743,11 @@ def reference_arm(a, rank, world):
     sc = make_scene(a)
     cam = make_camera(a, 0)
     cs = CpuScene(a, sc, cam)
-    t, spent, _ = cs.measure(a.steps, a.warmup)
+    t, spent, fwd = cs.measure(a.steps, a.warmup)
     v = round(1.0 / t, 5)
     base = {"value": v, "unit": "train-steps/s"}
     base.update(cs.describe(a.steps, spent))
+    base["hits_per_ray_sample"] = round(float(fwd["nhit"].mean()), 2)
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "train-steps/s", "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1000 * t, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded {a.scene} scene)",
@@ -749,9 +762,11 @@ def reference_arm(a, rank, world):
 def main():
     a = parse()
     if a.record_traffic:
-        csv_path, key = a.record_traffic[0], " ".join(a.record_traffic[1:2])
-        scale = float(a.record_traffic[2]) if len(a.record_traffic) > 2 else 1.0
-        print(json.dumps({key: record_traffic(csv_path, key, scale)}))
+        if len(a.record_traffic) < 3:
+            sys.exit("--record-traffic CSV KEY KERNEL [UNITS_SCALE]")
+        csv_path, key, kernel = a.record_traffic[:3]
+        scale = float(a.record_traffic[3]) if len(a.record_traffic) > 3 else 1.0
+        print(json.dumps({key: record_traffic(csv_path, key, kernel, scale)}))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

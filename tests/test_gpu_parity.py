@@ -99,8 +99,12 @@ def test_reference_scenes_forward_backward(oracle, golden, name):
     assert np.array_equal(g.was_visible.cpu().numpy()[:, 0], ref[:, 15] > 0)
 
 
-def test_snapshot_and_bvh_bit_exact(oracle):
-    sc = synthetic.clustered_scene(30_000, seed=3)
+@pytest.mark.parametrize("n", [30_000, 1_500_000])
+def test_snapshot_and_bvh_bit_exact(oracle, n):
+    """Snapshot records, Morton codes, sorted order, nodes and root box of a rebuild, then of a refit,
+    bit-exact against the oracle; 1.5M Gaussians make each digit's row of tile counts (733 tiles)
+    longer than one block-wide chunk of the row scan, and the refit's blocks many."""
+    sc = synthetic.clustered_scene(n, seed=3)
     rt = G.make_tracer(16, 16, sc.mean, sc.rotation, sc.scale, sc.opacity, channels=np.zeros((sc.n, 3), np.float32))
     geom, l2w, aabb, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, sc.scale, sc.opacity)
     ws = rt.scene_workspace()
