@@ -120,3 +120,18 @@ def test_oracle_gaussian_response_matches_reference_kernel(oracle, refk, p):
     assert rel_err(sf, ref_sf) <= 1e-5
     assert np.abs(g - ref_g).max() <= 1e-6
     assert np.abs(a - ref_a).max() <= 1e-6
+
+
+def test_fp16_alpha_keys_equal_the_reference_kernel(oracle, refk):
+    """The reference composites with alpha stored in fp16 (cuda/core/per_pixel_linked_list.h:29-31)
+    and computes alpha with fast-math expf; our alpha (the oracle's, bit-exact with the GPU's) rounds
+    to the same fp16 key as the reference kernel's for every live sample here, so the images' 3e-4
+    distance from the reference tests' FP64 loops is the reference's own fp16 storage."""
+    opac, hit = refk["kf_opacity"], refk["kf_local_hit"]
+    d = (hit.astype(np.float32) ** 2).sum(1, dtype=np.float32)
+    g = np.array([oracle.eval_gaussian(float(x), 2.0) for x in d], np.float32)
+    a = np.array([oracle.maxalpha_mul(float(x), float(o)) for x, o in zip(g, opac)], np.float32)
+    ref = refk["kf_p2.0_alpha"]
+    live = a > 0.01
+    assert live.sum() > 3000
+    assert np.array_equal(a[live].astype(np.float16), ref[live].astype(np.float16))
