@@ -158,3 +158,50 @@ def test_hit_list_overflow_raises_instead_of_trapping(gray_classes):
     rt.check_status()  # cleared
     torch.zeros(1, device="cuda").add_(1)
     torch.cuda.synchronize()
+
+
+def test_resolution_display_sh_degree_and_shrink_match_python_classes(gray_classes):
+    """The rest of the surface train.py and render.py use: a smaller render rectangle
+    (set_render_resolution), the SH-degree schedule (increment_sh_degree), display renders
+    (forward_pass_display) and pruning (resize to fewer Gaussians, then rebuild_bvh); every image is
+    identical to gray_gb300.classes on the same inputs."""
+    from gray_gb300 import classes
+
+    sc = synthetic.small_scene(seed=2, n=400)
+    cam = synthetic.camera_small(W, H, 64.0)
+    rts = [gray_classes.Raytracer(W, H, sc.n, 3, 1, 4_000_000, False),
+           classes.Raytracer(W, H, sc.n, 3, 1, 4_000_000, False)]
+    for rt in rts:
+        _setup(rt, sc)
+        rt.get_gaussians().current_sh_degree.fill_(0)
+
+    def frame(rt, w, h, display):
+        rt.set_render_resolution(w, h)
+        _camera(rt, cam)
+        if display:
+            with torch.no_grad():
+                rt.forward_pass_display()
+        else:
+            with torch.enable_grad():
+                rt.forward_pass()
+        return rt.get_framebuffer().output_channels[:h, :w].clone()
+
+    for step in range(4):
+        w, h = (W, H) if step % 2 == 0 else (40, 24)
+        imgs = [frame(rt, w, h, display=step == 3) for rt in rts]
+        torch.cuda.synchronize()
+        assert torch.equal(imgs[0], imgs[1]), step
+        for rt in rts:
+            rt.get_gaussians().increment_sh_degree()
+    assert int(rts[0].get_gaussians().current_sh_degree.item()) == 3
+    keep = sc.n // 3
+    for rt in rts:
+        rt.set_render_resolution(W, H)
+        rt.resize(keep)  # train.py prunes by compacting the holders, then shrinking them
+        rt.rebuild_bvh()
+    imgs = [frame(rt, W, H, display=False) for rt in rts]
+    torch.cuda.synchronize()
+    for rt in rts:
+        rt.check_status()
+    assert tuple(rts[0].get_gaussians().mean.shape) == (keep, 3)
+    assert torch.equal(imgs[0], imgs[1])
