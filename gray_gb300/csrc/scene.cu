@@ -1,5 +1,6 @@
 // scene.cu -- per-Gaussian kernels: instance snapshot, per-forward preparation (live opacity,
 // scaling factor, SH colour) and the post-backward gradient fold with the SH backward.
+#include "gray_bulk.cuh"
 #include "gray_device.cuh"
 #include "gray_internal.h"
 
@@ -79,20 +80,20 @@ __device__ __forceinline__ int sh_count(int degree) {
 // cuda/optix/bvh_wrapper.cu:8-59).  Writes the world->unit-sphere rows (M | mu), the
 // unit-sphere->world rows R diag(s), the leaf box and the visibility of each Gaussian.
 // ---------------------------------------------------------------------------------------------
-__global__ void snapshot_kernel(int n, const float *__restrict__ mean, const float4 *__restrict__ rotation,
-                                const float *__restrict__ scale, const float *__restrict__ opacity,
-                                const float *__restrict__ cfg_alpha_threshold, const float *__restrict__ cfg_exp_power,
-                                const float *__restrict__ cfg_gsf, float4 *__restrict__ geom, float4 *__restrict__ l2w,
-                                float4 *__restrict__ aabb, uint8_t *__restrict__ visible) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float athr = *cfg_alpha_threshold, p = *cfg_exp_power, gsf = *cfg_gsf;
-    float o = sigmoid_act(opacity[i]);
+// The snapshot of one Gaussian from its parameters (mean, rotation quaternion (r, x, y, z), log
+// scales, logit opacity): rows g of (M | mu), rows w of (L | mu), its leaf box and visibility.
+struct SnapRecord {
+    float4 g[3], w[3], bmin, bmax;
+    bool vis;
+};
+
+__device__ __forceinline__ void snapshot_one(const float mu_in[3], float4 q, const float log_s[3], float logit_o,
+                                             float athr, float p, float gsf, SnapRecord &out) {
+    float o = sigmoid_act(logit_o);
     float sf = scaling_factor(o, athr, p);
     float s[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) s[k] = gexp(scale[3 * i + k]) * sf * gsf;
-    float4 q = rotation[i];
+    for (int k = 0; k < 3; k++) s[k] = gexp(log_s[k]) * sf * gsf;
     float r = q.x, x = q.y, y = q.z, z = q.w;
     float norm = sqrtf(r * r + x * x + y * y + z * z);
     r = r / norm;
@@ -109,7 +110,7 @@ __global__ void snapshot_kernel(int n, const float *__restrict__ mean, const flo
     R[6] = 2.0f * (x * z - r * y);
     R[7] = 2.0f * (y * z + r * x);
     R[8] = 1.0f - 2.0f * (x * x + y * y);
-    float mu[3] = {mean[3 * i], mean[3 * i + 1], mean[3 * i + 2]};
+    const float mu[3] = {mu_in[0], mu_in[1], mu_in[2]};
     bool vis = sf > 0.0f && s[0] > 0.0f && s[1] > 0.0f && s[2] > 0.0f && isfinite(s[0]) && isfinite(s[1]) &&
                isfinite(s[2]) && isfinite(mu[0]) && isfinite(mu[1]) && isfinite(mu[2]);
     float L[9];
@@ -125,10 +126,9 @@ __global__ void snapshot_kernel(int n, const float *__restrict__ mean, const flo
         gr.y = vis ? R[3 + rr] / s[rr] : 0.0f;
         gr.z = vis ? R[6 + rr] / s[rr] : 0.0f;
         gr.w = mu[rr];
-        geom[3 * i + rr] = gr;
-        l2w[3 * i + rr] = make_float4(L[3 * rr], L[3 * rr + 1], L[3 * rr + 2], mu[rr]);
+        out.g[rr] = gr;
+        out.w[rr] = make_float4(L[3 * rr], L[3 * rr + 1], L[3 * rr + 2], mu[rr]);
     }
-    float4 bmin, bmax;
     if (vis) {
         float pad_mu = 2.0e-6f * (fabsf(mu[0]) + fabsf(mu[1]) + fabsf(mu[2]));
         float h[3];
@@ -138,25 +138,178 @@ __global__ void snapshot_kernel(int n, const float *__restrict__ mean, const flo
             float hh = sqrtf(a0 * a0 + a1 * a1 + a2 * a2);
             h[rr] = hh + hh * 1.0e-4f + pad_mu + 1.0e-30f;
         }
-        bmin = make_float4(mu[0] - h[0], mu[1] - h[1], mu[2] - h[2], 0.0f);
-        bmax = make_float4(mu[0] + h[0], mu[1] + h[1], mu[2] + h[2], 0.0f);
+        out.bmin = make_float4(mu[0] - h[0], mu[1] - h[1], mu[2] - h[2], 0.0f);
+        out.bmax = make_float4(mu[0] + h[0], mu[1] + h[1], mu[2] + h[2], 0.0f);
     } else {
         bool fin = isfinite(mu[0]) && isfinite(mu[1]) && isfinite(mu[2]);
-        bmin = fin ? make_float4(mu[0], mu[1], mu[2], 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        bmax = bmin;
+        out.bmin = fin ? make_float4(mu[0], mu[1], mu[2], 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        out.bmax = out.bmin;
     }
-    aabb[2 * i] = bmin;
-    aabb[2 * i + 1] = bmax;
-    visible[i] = vis ? 1 : 0;
+    out.vis = vis;
+}
+
+// One thread per Gaussian of [first, n): the short tail of the bulk-pipelined kernel, and the
+// whole snapshot when a pointer is not 16-byte aligned.
+__global__ void snapshot_kernel(int first, int n, const float *__restrict__ mean, const float4 *__restrict__ rotation,
+                                const float *__restrict__ scale, const float *__restrict__ opacity,
+                                const float *__restrict__ cfg_alpha_threshold, const float *__restrict__ cfg_exp_power,
+                                const float *__restrict__ cfg_gsf, float4 *__restrict__ geom, float4 *__restrict__ l2w,
+                                float4 *__restrict__ aabb, uint8_t *__restrict__ visible) {
+    const int i = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float mu[3] = {mean[3 * i], mean[3 * i + 1], mean[3 * i + 2]};
+    const float ls[3] = {scale[3 * i], scale[3 * i + 1], scale[3 * i + 2]};
+    SnapRecord r;
+    snapshot_one(mu, rotation[i], ls, opacity[i], *cfg_alpha_threshold, *cfg_exp_power, *cfg_gsf, r);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        geom[3 * i + k] = r.g[k];
+        l2w[3 * i + k] = r.w[k];
+    }
+    aabb[2 * i] = r.bmin;
+    aabb[2 * i + 1] = r.bmax;
+    visible[i] = r.vis ? 1 : 0;
+}
+
+// Bulk-pipelined snapshot: a persistent block takes tiles of kSnapTile consecutive Gaussians.  One
+// thread loads a tile's parameter rows (mean, rotation, scale, opacity: 44 B per Gaussian, four
+// contiguous ranges) into shared memory with bulk copies completing on an mbarrier, double-buffered
+// so that the next tile's loads are in flight while this one is computed; each thread computes one
+// Gaussian and writes its records into a shared-memory copy of the tile's output ranges, which one
+// thread then stores with four bulk copies (geom, l2w, aabb, visible: 129 B per Gaussian) while the
+// block goes on.  Every copy starts on a 16-byte boundary and spans a multiple of 16 bytes (the
+// launcher checks the pointers; the tile is a multiple of 16 Gaussians).  Gaussians past the last
+// full tile go to snapshot_kernel.
+constexpr int kSnapTile = 128;
+static_assert(kSnapTile % 16 == 0, "every per-tile range must span a multiple of 16 bytes");
+
+struct SnapIn {
+    float mean[3 * kSnapTile];
+    float4 rotation[kSnapTile];
+    float scale[3 * kSnapTile];
+    float opacity[kSnapTile];
+};
+struct SnapOut {
+    float4 geom[3 * kSnapTile];
+    float4 l2w[3 * kSnapTile];
+    float4 aabb[2 * kSnapTile];
+    uint8_t visible[kSnapTile];
+};
+constexpr uint32_t kSnapInBytes = 44u * kSnapTile;
+
+__device__ __forceinline__ void snap_issue_loads(SnapIn &in, uint64_t *bar, int tile, const float *mean,
+                                                 const float4 *rotation, const float *scale, const float *opacity) {
+    const size_t g0 = (size_t)tile * kSnapTile;
+    mbar_expect_tx(bar, kSnapInBytes);
+    bulk_load(in.mean, mean + 3 * g0, 12u * kSnapTile, bar);
+    bulk_load(in.rotation, rotation + g0, 16u * kSnapTile, bar);
+    bulk_load(in.scale, scale + 3 * g0, 12u * kSnapTile, bar);
+    bulk_load(in.opacity, opacity + g0, 4u * kSnapTile, bar);
+}
+
+__global__ void __launch_bounds__(kSnapTile) snapshot_bulk_kernel(
+    int tiles, const float *__restrict__ mean, const float4 *__restrict__ rotation, const float *__restrict__ scale,
+    const float *__restrict__ opacity, const float *__restrict__ cfg_alpha_threshold,
+    const float *__restrict__ cfg_exp_power, const float *__restrict__ cfg_gsf, float4 *__restrict__ geom,
+    float4 *__restrict__ l2w, float4 *__restrict__ aabb, uint8_t *__restrict__ visible, int32_t *__restrict__ status) {
+    __shared__ __align__(16) SnapIn in[2];
+    __shared__ __align__(16) SnapOut out;
+    __shared__ __align__(8) uint64_t bar[2];
+    const int t = threadIdx.x;
+    if (t == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const float athr = *cfg_alpha_threshold, pw = *cfg_exp_power, gsf = *cfg_gsf;
+    int tile = blockIdx.x;
+    if (t == 0 && tile < tiles) snap_issue_loads(in[0], &bar[0], tile, mean, rotation, scale, opacity);
+    int it = 0;
+    bool timed_out = false;
+    for (; tile < tiles; it++, tile += gridDim.x) {
+        const int st = it & 1;
+        const int next = tile + gridDim.x;
+        if (t == 0 && next < tiles) {
+            // in[st ^ 1] was last read in the previous tile, before its barriers
+            fence_proxy_async();
+            snap_issue_loads(in[st ^ 1], &bar[st ^ 1], next, mean, rotation, scale, opacity);
+        }
+        const bool ok = __syncthreads_and(mbar_wait(&bar[st], (uint32_t)(it >> 1) & 1u, kBulkWaitNs));
+        if (!ok) {
+            if (t == 0) atomicOr(status, GRAY_STATUS_COPY_TIMEOUT);
+            timed_out = true;
+            break;
+        }
+        SnapRecord r;
+        {
+            const float mu[3] = {in[st].mean[3 * t], in[st].mean[3 * t + 1], in[st].mean[3 * t + 2]};
+            const float ls[3] = {in[st].scale[3 * t], in[st].scale[3 * t + 1], in[st].scale[3 * t + 2]};
+            snapshot_one(mu, in[st].rotation[t], ls, in[st].opacity[t], athr, pw, gsf, r);
+        }
+        if (t == 0) bulk_wait_read();  // the previous tile's stores have read the staging
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            out.geom[3 * t + k] = r.g[k];
+            out.l2w[3 * t + k] = r.w[k];
+        }
+        out.aabb[2 * t] = r.bmin;
+        out.aabb[2 * t + 1] = r.bmax;
+        out.visible[t] = r.vis ? 1 : 0;
+        fence_proxy_async();
+        __syncthreads();
+        if (t == 0) {
+            const size_t g0 = (size_t)tile * kSnapTile;
+            bulk_store(geom + 3 * g0, out.geom, 48u * kSnapTile);
+            bulk_store(l2w + 3 * g0, out.l2w, 48u * kSnapTile);
+            bulk_store(aabb + 2 * g0, out.aabb, 32u * kSnapTile);
+            bulk_store(visible + g0, out.visible, kSnapTile);
+            bulk_commit();
+        }
+    }
+    if (t == 0) {
+        bulk_wait_all();
+        if (timed_out) {
+            // the loads still in flight (this tile's and the next one's) get their own bounded
+            // waits, so that no copy targets this block's shared memory after it exits
+            mbar_wait(&bar[it & 1], (uint32_t)(it >> 1) & 1u, kBulkWaitNs);
+            if (tile + (int)gridDim.x < tiles)
+                mbar_wait(&bar[(it + 1) & 1], (uint32_t)((it + 1) >> 1) & 1u, kBulkWaitNs);
+        }
+    }
 }
 
 cudaError_t launch_snapshot(const gray_params &p, cudaStream_t s) {
     const gray_gaussians &g = p.gaussians;
-    if (g.count <= 0) return cudaSuccess;
-    snapshot_kernel<<<blocks_for(g.count), kThreads, 0, s>>>(
-        g.count, g.mean, reinterpret_cast<const float4 *>(g.rotation), g.scale, g.opacity, p.config.alpha_threshold,
-        p.config.exp_power, p.config.global_scale_factor, reinterpret_cast<float4 *>(p.scene.geom),
-        reinterpret_cast<float4 *>(p.scene.l2w), reinterpret_cast<float4 *>(p.scene.aabb), p.scene.visible);
+    const int n = g.count;
+    if (n <= 0) return cudaSuccess;
+    const float4 *rot = reinterpret_cast<const float4 *>(g.rotation);
+    float4 *geom = reinterpret_cast<float4 *>(p.scene.geom), *l2w = reinterpret_cast<float4 *>(p.scene.l2w),
+           *aabb = reinterpret_cast<float4 *>(p.scene.aabb);
+    const bool bulk = p.status && aligned16(g.mean) && aligned16(g.rotation) && aligned16(g.scale) &&
+                      aligned16(g.opacity) && aligned16(geom) && aligned16(l2w) && aligned16(aabb) &&
+                      aligned16(p.scene.visible);
+    const int tiles = bulk ? n / kSnapTile : 0;
+    if (tiles > 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaError_t e;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, snapshot_bulk_kernel, kSnapTile, 0)) !=
+            cudaSuccess)
+            return e;
+        const int want = sms * (per_sm > 0 ? per_sm : 1);
+        snapshot_bulk_kernel<<<tiles < want ? tiles : want, kSnapTile, 0, s>>>(
+            tiles, g.mean, rot, g.scale, g.opacity, p.config.alpha_threshold, p.config.exp_power,
+            p.config.global_scale_factor, geom, l2w, aabb, p.scene.visible, p.status);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    const int first = tiles * kSnapTile;
+    if (first < n)
+        snapshot_kernel<<<blocks_for(n - first), kThreads, 0, s>>>(
+            first, n, g.mean, rot, g.scale, g.opacity, p.config.alpha_threshold, p.config.exp_power,
+            p.config.global_scale_factor, geom, l2w, aabb, p.scene.visible);
     return cudaGetLastError();
 }
 
@@ -179,19 +332,46 @@ __device__ __forceinline__ float sh_load<__half>(const __half *p) {
     return __half2float(*p);
 }
 
+// SH colour of one Gaussian seen from cam (reference: sh_forward_kernel, cuda/utils/sh.cu:224-247);
+// dc and row (its 3 * nb rest coefficients, coefficient-major) in the storage type.
+template <typename SHT>
+__device__ __forceinline__ void sh_colour(const float mu[3], const float *cam, const SHT *dc, const SHT *row, int nb,
+                                          float out[3]) {
+    float v[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) v[k] = mu[k] - cam[k];
+    float len2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    float inv = 1.0f / sqrtf(fmaxf(len2, 1e-20f));
+    float b[15];
+    sh_basis(v[0] * inv, v[1] * inv, v[2] * inv, b);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float acc = SH_C0 * sh_load<SHT>(dc + c);
+#pragma unroll
+        for (int j = 0; j < 15; j++)
+            if (j < nb) acc = fmaf(b[j], sh_load<SHT>(row + 3 * j + c), acc);
+        acc = acc + 0.5f;
+        out[c] = fmaxf(acc, 0.0f);
+    }
+}
+
+// One thread per Gaussian of [first, n), SH rows staged through shared memory with coalesced loads:
+// the tail of the bulk-pipelined kernel, and the whole pass when a pointer is not 16-byte aligned.
+// count_call: this launch counts the forward call and empties the backward hit list.
 template <typename SHT>
 __global__ void __launch_bounds__(kPrepThreads) forward_prep_kernel(
-    int n, int num_rest, const float *__restrict__ opacity, const uint8_t *__restrict__ visible,
+    int first, int n, int num_rest, const float *__restrict__ opacity, const uint8_t *__restrict__ visible,
     const float *__restrict__ cfg_alpha_threshold, const float *__restrict__ cfg_exp_power,
     const uint8_t *__restrict__ cfg_enable_sh, const int32_t *__restrict__ current_sh_degree, int max_sh_degree,
     const float *__restrict__ mean, const float *__restrict__ cam_origin, const SHT *__restrict__ sh_dc,
     const SHT *__restrict__ sh_rest, float *__restrict__ channels, float2 *__restrict__ live,
     uint8_t *__restrict__ was_visible, uint32_t *__restrict__ total_num_calls, uint32_t *__restrict__ hit_counter,
-    int reset_frame) {
-    extern __shared__ float stage[];  // kPrepThreads * num_rest * 3 floats
-    const int i0 = blockIdx.x * kPrepThreads;
+    int reset_frame, int count_call) {
+    extern __shared__ __align__(16) unsigned char prep_smem[];
+    SHT *stage = reinterpret_cast<SHT *>(prep_smem);  // kPrepThreads * num_rest * 3 coefficients
+    const int i0 = first + blockIdx.x * kPrepThreads;
     const int i = i0 + threadIdx.x;
-    if (reset_frame && blockIdx.x == 0 && threadIdx.x == 0) {
+    if (count_call && blockIdx.x == 0 && threadIdx.x == 0) {
         *total_num_calls += 1u;
         *hit_counter = 0u;
     }
@@ -199,12 +379,11 @@ __global__ void __launch_bounds__(kPrepThreads) forward_prep_kernel(
     int degree = *current_sh_degree;
     degree = min(min(degree, 3), max_sh_degree);
     const int nb = enable_sh ? sh_count(degree) : 0;
+    const int per = num_rest * 3;
     if (nb > 0) {
-        // coalesced staging of this block's rows of sh_rest ([n, num_rest, 3])
         const int rows = min(kPrepThreads, n - i0);
-        const int per = num_rest * 3;
         const long long base = (long long)i0 * per;
-        for (int t = threadIdx.x; t < rows * per; t += kPrepThreads) stage[t] = sh_load<SHT>(sh_rest + base + t);
+        for (int t = threadIdx.x; t < rows * per; t += kPrepThreads) stage[t] = sh_rest[base + t];
     }
     __syncthreads();
     if (i >= n) return;
@@ -214,23 +393,178 @@ __global__ void __launch_bounds__(kPrepThreads) forward_prep_kernel(
     float sf = scaling_factor(o, athr, pw);
     live[i] = make_float2(visible[i] ? o : __int_as_float(0xff800000), sf);
     if (!enable_sh) return;
-    float v[3];
+    const float mu[3] = {mean[3 * i], mean[3 * i + 1], mean[3 * i + 2]};
+    float col[3];
+    sh_colour<SHT>(mu, cam_origin, sh_dc + 3 * i, stage + threadIdx.x * per, nb, col);
 #pragma unroll
-    for (int k = 0; k < 3; k++) v[k] = mean[3 * i + k] - cam_origin[k];
-    float len2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
-    float inv = 1.0f / sqrtf(fmaxf(len2, 1e-20f));
-    float b[15];
-    sh_basis(v[0] * inv, v[1] * inv, v[2] * inv, b);
-    const float *row = stage + threadIdx.x * num_rest * 3;
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        float acc = SH_C0 * sh_load<SHT>(sh_dc + 3 * i + c);
-#pragma unroll
-        for (int j = 0; j < 15; j++)
-            if (j < nb) acc = fmaf(b[j], row[3 * j + c], acc);
-        acc = acc + 0.5f;
-        channels[3 * i + c] = fmaxf(acc, 0.0f);
+    for (int c = 0; c < 3; c++) channels[3 * i + c] = col[c];
+}
+
+// Bulk-pipelined forward preparation: a persistent block takes tiles of kPrepTile consecutive
+// Gaussians; one thread loads a tile's inputs (opacity, mean, snapshot visibility, and with SH on
+// the DC and rest coefficients: contiguous ranges) into one of two shared-memory stages with bulk
+// copies completing on an mbarrier, so the next tile's loads are in flight while this one is
+// computed; each thread computes one Gaussian into a shared-memory copy of the tile's outputs
+// (live values, colours, the reset visited flags), stored by one thread with bulk copies.  Stage
+// layout (byte offsets, T = kPrepTile, b = sizeof(SHT)): opacity 0, mean 4T, visible 16T, sh_dc 17T,
+// sh_rest 17T + 3Tb; every range spans a multiple of 16 bytes.  Shared memory: 16 B of barriers,
+// two stages, then the output copy (colours 12T, live 8T, flags T).
+constexpr int kPrepTile = 64;
+static_assert(kPrepTile % 16 == 0, "every per-tile range must span a multiple of 16 bytes");
+
+__host__ __device__ __forceinline__ uint32_t prep_stage_bytes(int num_rest, uint32_t sb) {
+    return 17u * kPrepTile + 3u * kPrepTile * sb + (uint32_t)kPrepTile * 3u * (uint32_t)num_rest * sb;
+}
+__host__ __device__ __forceinline__ uint32_t prep_smem_bytes(int num_rest, uint32_t sb) {
+    return 16u + 2u * prep_stage_bytes(num_rest, sb) + 21u * kPrepTile;
+}
+
+template <typename SHT>
+__device__ __forceinline__ void prep_issue_loads(unsigned char *stg, uint64_t *bar, int tile, int per, bool dc,
+                                                 bool rest, const float *opacity, const float *mean,
+                                                 const uint8_t *visible, const SHT *sh_dc, const SHT *sh_rest) {
+    constexpr uint32_t T = kPrepTile, sb = sizeof(SHT);
+    const size_t g0 = (size_t)tile * T;
+    const uint32_t rest_bytes = T * (uint32_t)per * sb;
+    mbar_expect_tx(bar, 17u * T + (dc ? 3u * T * sb : 0u) + (rest ? rest_bytes : 0u));
+    bulk_load(stg, opacity + g0, 4u * T, bar);
+    bulk_load(stg + 4 * T, mean + 3 * g0, 12u * T, bar);
+    bulk_load(stg + 16 * T, visible + g0, T, bar);
+    if (dc) bulk_load(stg + 17 * T, sh_dc + 3 * g0, 3u * T * sb, bar);
+    if (rest) bulk_load(stg + 17 * T + 3 * T * sb, sh_rest + g0 * per, rest_bytes, bar);
+}
+
+template <typename SHT>
+__global__ void __launch_bounds__(kPrepTile) forward_prep_bulk_kernel(
+    int tiles, int num_rest, const float *__restrict__ opacity, const uint8_t *__restrict__ visible,
+    const float *__restrict__ cfg_alpha_threshold, const float *__restrict__ cfg_exp_power,
+    const uint8_t *__restrict__ cfg_enable_sh, const int32_t *__restrict__ current_sh_degree, int max_sh_degree,
+    const float *__restrict__ mean, const float *__restrict__ cam_origin, const SHT *__restrict__ sh_dc,
+    const SHT *__restrict__ sh_rest, float *__restrict__ channels, float2 *__restrict__ live,
+    uint8_t *__restrict__ was_visible, uint32_t *__restrict__ total_num_calls, uint32_t *__restrict__ hit_counter,
+    int reset_frame, int32_t *__restrict__ status) {
+    constexpr uint32_t T = kPrepTile, sb = sizeof(SHT);
+    extern __shared__ __align__(16) unsigned char prep_smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(prep_smem);
+    const int per = 3 * num_rest;
+    const uint32_t stage_bytes = prep_stage_bytes(num_rest, sb);
+    unsigned char *stages = prep_smem + 16;
+    unsigned char *outb = stages + 2 * stage_bytes;
+    float *ch_out = reinterpret_cast<float *>(outb);
+    float2 *live_out = reinterpret_cast<float2 *>(outb + 12 * T);
+    uint8_t *wv_out = outb + 20 * T;
+    const int t = threadIdx.x;
+    if (reset_frame && blockIdx.x == 0 && t == 0) {
+        *total_num_calls += 1u;
+        *hit_counter = 0u;
     }
+    const bool enable_sh = *cfg_enable_sh != 0;
+    int degree = *current_sh_degree;
+    degree = min(min(degree, 3), max_sh_degree);
+    const int nb = enable_sh ? sh_count(degree) : 0;
+    const float athr = *cfg_alpha_threshold, pw = *cfg_exp_power;
+    const float cam[3] = {cam_origin[0], cam_origin[1], cam_origin[2]};
+    if (t == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    int tile = blockIdx.x;
+    if (t == 0 && tile < tiles)
+        prep_issue_loads<SHT>(stages, &bar[0], tile, per, enable_sh, nb > 0, opacity, mean, visible, sh_dc, sh_rest);
+    int it = 0;
+    bool timed_out = false;
+    for (; tile < tiles; it++, tile += gridDim.x) {
+        const int st = it & 1;
+        const int next = tile + gridDim.x;
+        if (t == 0 && next < tiles) {
+            fence_proxy_async();  // stage st ^ 1 was last read in the previous tile, before its barriers
+            prep_issue_loads<SHT>(stages + (st ^ 1) * stage_bytes, &bar[st ^ 1], next, per, enable_sh, nb > 0,
+                                  opacity, mean, visible, sh_dc, sh_rest);
+        }
+        const bool ok = __syncthreads_and(mbar_wait(&bar[st], (uint32_t)(it >> 1) & 1u, kBulkWaitNs));
+        if (!ok) {
+            if (t == 0) atomicOr(status, GRAY_STATUS_COPY_TIMEOUT);
+            timed_out = true;
+            break;
+        }
+        const unsigned char *stg = stages + st * stage_bytes;
+        const float o = sigmoid_act(reinterpret_cast<const float *>(stg)[t]);
+        const float sf = scaling_factor(o, athr, pw);
+        const float2 lv = make_float2(stg[16 * T + t] ? o : __int_as_float(0xff800000), sf);
+        float col[3] = {0.0f, 0.0f, 0.0f};
+        if (enable_sh) {
+            const float *m = reinterpret_cast<const float *>(stg + 4 * T) + 3 * t;
+            const float mu[3] = {m[0], m[1], m[2]};
+            const SHT *dc = reinterpret_cast<const SHT *>(stg + 17 * T) + 3 * t;
+            const SHT *row = reinterpret_cast<const SHT *>(stg + 17 * T + 3 * T * sb) + per * t;
+            sh_colour<SHT>(mu, cam, dc, row, nb, col);
+        }
+        if (t == 0) bulk_wait_read();  // the previous tile's stores have read the output copy
+        __syncthreads();
+        live_out[t] = lv;
+#pragma unroll
+        for (int c = 0; c < 3; c++) ch_out[3 * t + c] = col[c];
+        wv_out[t] = 0;
+        fence_proxy_async();
+        __syncthreads();
+        if (t == 0) {
+            const size_t g0 = (size_t)tile * T;
+            bulk_store(live + g0, live_out, 8u * T);
+            if (enable_sh) bulk_store(channels + 3 * g0, ch_out, 12u * T);
+            if (reset_frame) bulk_store(was_visible + g0, wv_out, T);
+            bulk_commit();
+        }
+    }
+    if (t == 0) {
+        bulk_wait_all();
+        if (timed_out) {
+            // bounded waits for the loads still in flight before the block's shared memory goes
+            mbar_wait(&bar[it & 1], (uint32_t)(it >> 1) & 1u, kBulkWaitNs);
+            if (tile + (int)gridDim.x < tiles)
+                mbar_wait(&bar[(it + 1) & 1], (uint32_t)((it + 1) >> 1) & 1u, kBulkWaitNs);
+        }
+    }
+}
+
+template <typename SHT>
+static cudaError_t forward_prep_typed(const gray_params &p, bool reset_frame, cudaStream_t s) {
+    const gray_gaussians &g = p.gaussians;
+    const int n = g.count, num_rest = g.num_sh_coeffs;
+    const SHT *dc = reinterpret_cast<const SHT *>(g.sh_coeffs_dc);
+    const SHT *rest = reinterpret_cast<const SHT *>(g.sh_coeffs_rest);
+    float2 *live = reinterpret_cast<float2 *>(p.scene.live);
+    const uint32_t smem = prep_smem_bytes(num_rest, sizeof(SHT));
+    const bool bulk = p.status && smem <= 48u * 1024u && aligned16(g.opacity) && aligned16(g.mean) &&
+                      aligned16(p.scene.visible) && aligned16(dc) && (num_rest == 0 || aligned16(rest)) &&
+                      aligned16(g.channels) && aligned16(live) && aligned16(g.was_visible);
+    const int tiles = bulk ? n / kPrepTile : 0;
+    cudaError_t e;
+    if (tiles > 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forward_prep_bulk_kernel<SHT>, kPrepTile,
+                                                               smem)) != cudaSuccess)
+            return e;
+        const int want = sms * (per_sm > 0 ? per_sm : 1);
+        forward_prep_bulk_kernel<SHT><<<tiles < want ? tiles : want, kPrepTile, smem, s>>>(
+            tiles, num_rest, g.opacity, p.scene.visible, p.config.alpha_threshold, p.config.exp_power,
+            p.config.enable_sh, g.current_sh_degree, g.max_sh_degree, g.mean, p.camera.origin, dc, rest, g.channels,
+            live, g.was_visible, p.metadata.total_num_calls, p.hitlist.total_words, reset_frame ? 1 : 0, p.status);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    const int first = tiles * kPrepTile;
+    if (first < n) {
+        const size_t tail_smem = (size_t)kPrepThreads * (size_t)(num_rest > 0 ? num_rest : 1) * 3 * sizeof(SHT);
+        forward_prep_kernel<SHT><<<blocks_for(n - first, kPrepThreads), kPrepThreads, tail_smem, s>>>(
+            first, n, num_rest, g.opacity, p.scene.visible, p.config.alpha_threshold, p.config.exp_power,
+            p.config.enable_sh, g.current_sh_degree, g.max_sh_degree, g.mean, p.camera.origin, dc, rest, g.channels,
+            live, g.was_visible, p.metadata.total_num_calls, p.hitlist.total_words, reset_frame ? 1 : 0,
+            reset_frame && tiles == 0 ? 1 : 0);
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_forward_prep(const gray_params &p, bool reset_frame, cudaStream_t s) {
@@ -241,25 +575,7 @@ cudaError_t launch_forward_prep(const gray_params &p, bool reset_frame, cudaStre
         return e;
     }
     if (g.count <= 0) return cudaSuccess;
-    const int num_rest = g.num_sh_coeffs;
-    const size_t smem = (size_t)kPrepThreads * (size_t)(num_rest > 0 ? num_rest : 1) * 3 * sizeof(float);
-    const unsigned int blocks = blocks_for(g.count, kPrepThreads);
-    if (g.sh_is_fp16) {
-        forward_prep_kernel<__half><<<blocks, kPrepThreads, smem, s>>>(
-            g.count, num_rest, g.opacity, p.scene.visible, p.config.alpha_threshold, p.config.exp_power,
-            p.config.enable_sh, g.current_sh_degree, g.max_sh_degree, g.mean, p.camera.origin,
-            reinterpret_cast<const __half *>(g.sh_coeffs_dc), reinterpret_cast<const __half *>(g.sh_coeffs_rest),
-            g.channels, reinterpret_cast<float2 *>(p.scene.live), g.was_visible, p.metadata.total_num_calls,
-            p.hitlist.total_words, reset_frame ? 1 : 0);
-    } else {
-        forward_prep_kernel<float><<<blocks, kPrepThreads, smem, s>>>(
-            g.count, num_rest, g.opacity, p.scene.visible, p.config.alpha_threshold, p.config.exp_power,
-            p.config.enable_sh, g.current_sh_degree, g.max_sh_degree, g.mean, p.camera.origin,
-            reinterpret_cast<const float *>(g.sh_coeffs_dc), reinterpret_cast<const float *>(g.sh_coeffs_rest),
-            g.channels, reinterpret_cast<float2 *>(p.scene.live), g.was_visible, p.metadata.total_num_calls,
-            p.hitlist.total_words, reset_frame ? 1 : 0);
-    }
-    return cudaGetLastError();
+    return g.sh_is_fp16 ? forward_prep_typed<__half>(p, reset_frame, s) : forward_prep_typed<float>(p, reset_frame, s);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -22,6 +22,7 @@
 //   recomputes alpha in fp32 and reduces the 16 per-hit gradient values into the per-Gaussian
 //   accumulator: lanes holding the same Gaussian combine in a tree, and the lowest issues four
 //   16-byte vector reductions.
+#include "gray_bulk.cuh"
 #include "gray_device.cuh"
 #include "gray_internal.h"
 
@@ -1715,31 +1716,132 @@ __device__ __forceinline__ void reduce_hit(float *row, uint32_t gid, float (&v)[
 // cuda/backward_pass.cu:101-111) and qn = q / |q|.
 constexpr int kRecVec = 6;
 
-__global__ void __launch_bounds__(256) bwd_record_kernel(int n, const float2 *__restrict__ live,
+__device__ __forceinline__ void bwd_record_one(float2 lv, const float log_s[3], float4 q, const float ch[3], float4 L0,
+                                               float4 L1, float4 L2, float eps, float4 r[kRecVec]) {
+    const float sf = lv.y;
+    float s[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) s[k] = gexp(log_s[k]);
+    const float qlen = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+    const float d0 = s[0] * sf + eps, d1 = s[1] * sf + eps, d2 = s[2] * sf + eps;
+    r[0] = make_float4(lv.x, sf, 1.0f / qlen, s[0]);
+    r[1] = make_float4(s[1], s[2], ch[0], ch[1]);
+    r[2] = make_float4(ch[2], L0.x / d0 * s[0], L0.y / d1 * s[1], L0.z / d2 * s[2]);
+    r[3] = make_float4(L1.x / d0 * s[0], L1.y / d1 * s[1], L1.z / d2 * s[2], L2.x / d0 * s[0]);
+    r[4] = make_float4(L2.y / d1 * s[1], L2.z / d2 * s[2], 0.0f, 0.0f);
+    r[5] = make_float4(q.x / qlen, q.y / qlen, q.z / qlen, q.w / qlen);
+}
+
+// One thread per Gaussian of [first, n): the tail of the bulk-pipelined kernel, and the whole pass
+// when a pointer is not 16-byte aligned.
+__global__ void __launch_bounds__(256) bwd_record_kernel(int first, int n, const float2 *__restrict__ live,
                                                          const float *__restrict__ scale,
                                                          const float4 *__restrict__ rotation,
                                                          const float *__restrict__ channels,
                                                          const float4 *__restrict__ l2w,
                                                          const float *__restrict__ eps_scale_grad,
                                                          float4 *__restrict__ rec) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = first + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float2 lv = live[i];
-    const float sf = lv.y, eps = *eps_scale_grad;
-    float s[3];
+    const float ls[3] = {scale[3 * i], scale[3 * i + 1], scale[3 * i + 2]};
+    const float ch[3] = {channels[3 * i], channels[3 * i + 1], channels[3 * i + 2]};
+    float4 r[kRecVec];
+    bwd_record_one(live[i], ls, rotation[i], ch, l2w[3 * i], l2w[3 * i + 1], l2w[3 * i + 2], *eps_scale_grad, r);
+    float4 *o = rec + kRecVec * (size_t)i;
 #pragma unroll
-    for (int k = 0; k < 3; k++) s[k] = gexp(scale[3 * i + k]);
-    const float4 q = rotation[i];
-    const float qlen = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
-    const float4 L0 = l2w[3 * i], L1 = l2w[3 * i + 1], L2 = l2w[3 * i + 2];
-    const float d0 = s[0] * sf + eps, d1 = s[1] * sf + eps, d2 = s[2] * sf + eps;
-    float4 *r = rec + kRecVec * (size_t)i;
-    r[0] = make_float4(lv.x, sf, 1.0f / qlen, s[0]);
-    r[1] = make_float4(s[1], s[2], channels[3 * i], channels[3 * i + 1]);
-    r[2] = make_float4(channels[3 * i + 2], L0.x / d0 * s[0], L0.y / d1 * s[1], L0.z / d2 * s[2]);
-    r[3] = make_float4(L1.x / d0 * s[0], L1.y / d1 * s[1], L1.z / d2 * s[2], L2.x / d0 * s[0]);
-    r[4] = make_float4(L2.y / d1 * s[1], L2.z / d2 * s[2], 0.0f, 0.0f);
-    r[5] = make_float4(q.x / qlen, q.y / qlen, q.z / qlen, q.w / qlen);
+    for (int k = 0; k < kRecVec; k++) o[k] = r[k];
+}
+
+// Bulk-pipelined record pass: persistent blocks take tiles of kRecTile Gaussians; one thread loads
+// a tile's inputs (live, scale, rotation, channels, l2w rows: 96 B per Gaussian, five contiguous
+// ranges) into one of two shared-memory stages with bulk copies completing on an mbarrier, so the
+// next tile's loads are in flight while this one is computed, and stores the tile's records (96 B
+// per Gaussian) from a shared-memory copy with one bulk copy.  Every copy starts on a 16-byte
+// boundary and spans a multiple of 16 bytes (the launcher checks the pointers).
+constexpr int kRecTile = 128;
+static_assert(kRecTile % 16 == 0, "every per-tile range must span a multiple of 16 bytes");
+
+struct RecIn {
+    float4 l2w[3 * kRecTile];
+    float4 rotation[kRecTile];
+    float2 live[kRecTile];
+    float scale[3 * kRecTile];
+    float channels[3 * kRecTile];
+};
+constexpr uint32_t kRecInBytes = 96u * kRecTile;
+
+__device__ __forceinline__ void rec_issue_loads(RecIn &in, uint64_t *bar, int tile, const float2 *live,
+                                                const float *scale, const float4 *rotation, const float *channels,
+                                                const float4 *l2w) {
+    const size_t g0 = (size_t)tile * kRecTile;
+    mbar_expect_tx(bar, kRecInBytes);
+    bulk_load(in.l2w, l2w + 3 * g0, 48u * kRecTile, bar);
+    bulk_load(in.rotation, rotation + g0, 16u * kRecTile, bar);
+    bulk_load(in.live, live + g0, 8u * kRecTile, bar);
+    bulk_load(in.scale, scale + 3 * g0, 12u * kRecTile, bar);
+    bulk_load(in.channels, channels + 3 * g0, 12u * kRecTile, bar);
+}
+
+__global__ void __launch_bounds__(kRecTile) bwd_record_bulk_kernel(
+    int tiles, const float2 *__restrict__ live, const float *__restrict__ scale, const float4 *__restrict__ rotation,
+    const float *__restrict__ channels, const float4 *__restrict__ l2w, const float *__restrict__ eps_scale_grad,
+    float4 *__restrict__ rec, int32_t *__restrict__ status) {
+    __shared__ __align__(16) RecIn in[2];
+    __shared__ __align__(16) float4 out[kRecVec * kRecTile];
+    __shared__ __align__(8) uint64_t bar[2];
+    const int t = threadIdx.x;
+    if (t == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const float eps = *eps_scale_grad;
+    int tile = blockIdx.x;
+    if (t == 0 && tile < tiles) rec_issue_loads(in[0], &bar[0], tile, live, scale, rotation, channels, l2w);
+    int it = 0;
+    bool timed_out = false;
+    for (; tile < tiles; it++, tile += gridDim.x) {
+        const int st = it & 1;
+        const int next = tile + gridDim.x;
+        if (t == 0 && next < tiles) {
+            fence_proxy_async();  // in[st ^ 1] was last read in the previous tile, before its barriers
+            rec_issue_loads(in[st ^ 1], &bar[st ^ 1], next, live, scale, rotation, channels, l2w);
+        }
+        const bool ok = __syncthreads_and(mbar_wait(&bar[st], (uint32_t)(it >> 1) & 1u, kBulkWaitNs));
+        if (!ok) {
+            if (t == 0) atomicOr(status, GRAY_STATUS_COPY_TIMEOUT);
+            timed_out = true;
+            break;
+        }
+        float4 r[kRecVec];
+        {
+            const RecIn &x = in[st];
+            const float ls[3] = {x.scale[3 * t], x.scale[3 * t + 1], x.scale[3 * t + 2]};
+            const float ch[3] = {x.channels[3 * t], x.channels[3 * t + 1], x.channels[3 * t + 2]};
+            bwd_record_one(x.live[t], ls, x.rotation[t], ch, x.l2w[3 * t], x.l2w[3 * t + 1], x.l2w[3 * t + 2], eps,
+                           r);
+        }
+        if (t == 0) bulk_wait_read();  // the previous tile's store has read the output copy
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kRecVec; k++) out[kRecVec * t + k] = r[k];
+        fence_proxy_async();
+        __syncthreads();
+        if (t == 0) {
+            bulk_store(rec + kRecVec * (size_t)tile * kRecTile, out, 16u * kRecVec * kRecTile);
+            bulk_commit();
+        }
+    }
+    if (t == 0) {
+        bulk_wait_all();
+        if (timed_out) {
+            // bounded waits for the loads still in flight before the block's shared memory goes
+            mbar_wait(&bar[it & 1], (uint32_t)(it >> 1) & 1u, kBulkWaitNs);
+            if (tile + (int)gridDim.x < tiles)
+                mbar_wait(&bar[(it + 1) & 1], (uint32_t)((it + 1) >> 1) & 1u, kBulkWaitNs);
+        }
+    }
 }
 
 // What one composited hit reads: the snapshot rows and the backward record (9 x 16 B).
@@ -1908,13 +2010,32 @@ __global__ void __launch_bounds__(128) trace_backward_kernel(const BwdArgs a) {
 cudaError_t launch_trace_backward(const gray_params &p, cudaStream_t s) {
     const int n = p.gaussians.count;
     if (n > 0) {
-        bwd_record_kernel<<<(unsigned int)((n + 255) / 256), 256, 0, s>>>(
-            n, reinterpret_cast<const float2 *>(p.scene.live), p.gaussians.scale,
-            reinterpret_cast<const float4 *>(p.gaussians.rotation), p.gaussians.channels,
-            reinterpret_cast<const float4 *>(p.scene.l2w), p.config.eps_scale_grad,
-            reinterpret_cast<float4 *>(p.scene.bwd_rec));
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
+        const float2 *live = reinterpret_cast<const float2 *>(p.scene.live);
+        const float4 *rot = reinterpret_cast<const float4 *>(p.gaussians.rotation);
+        const float4 *l2w = reinterpret_cast<const float4 *>(p.scene.l2w);
+        float4 *rec = reinterpret_cast<float4 *>(p.scene.bwd_rec);
+        const bool bulk = p.status && aligned16(live) && aligned16(p.gaussians.scale) && aligned16(rot) &&
+                          aligned16(p.gaussians.channels) && aligned16(l2w) && aligned16(rec);
+        const int tiles = bulk ? n / kRecTile : 0;
+        cudaError_t e;
+        if (tiles > 0) {
+            int dev = 0, sms = 0, per_sm = 0;
+            if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+            if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bwd_record_bulk_kernel, kRecTile, 0)) !=
+                cudaSuccess)
+                return e;
+            const int want = sms * (per_sm > 0 ? per_sm : 1);
+            bwd_record_bulk_kernel<<<tiles < want ? tiles : want, kRecTile, 0, s>>>(
+                tiles, live, p.gaussians.scale, rot, p.gaussians.channels, l2w, p.config.eps_scale_grad, rec,
+                p.status);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
+        const int first = tiles * kRecTile;
+        if (first < n)
+            bwd_record_kernel<<<(unsigned int)((n - first + 255) / 256), 256, 0, s>>>(
+                first, n, live, p.gaussians.scale, rot, p.gaussians.channels, l2w, p.config.eps_scale_grad, rec);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     BwdArgs a;
     a.alloc_w = p.image_width;

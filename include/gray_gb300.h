@@ -44,6 +44,8 @@ extern "C" {
 #define GRAY_STATUS_REFIT_TIMEOUT 4       /* bottom-up refit spin budget exhausted */
 #define GRAY_STATUS_BAD_MODE 8            /* render_ellipsoids set on a forward with gradients enabled
                                              (reference: assertion, gray/raytracer.py:142-144) */
+#define GRAY_STATUS_COPY_TIMEOUT 16       /* a bulk (TMA) copy of a streaming kernel did not complete
+                                             within its wait limit; the kernel stopped early */
 
 /* Gaussian parameters and optimiser state (cuda/core/gaussians.h:7-65). */
 typedef struct gray_gaussians {

@@ -142,6 +142,39 @@ def test_snapshot_and_bvh_bit_exact(oracle, n):
     assert np.array_equal(ws.root_box.cpu().numpy(), tree.root_box)
 
 
+@pytest.mark.parametrize("n", [63, 64, 129, 200_003])
+@pytest.mark.parametrize("fp16", [False, True])
+def test_forward_prep_tiles_bit_exact(oracle, n, fp16):
+    """Live values (opacity, scaling factor; -inf opacity where the snapshot is invisible), SH colours
+    at degrees 0-3 and the reset visited flags of the per-forward preparation, bit-exact against the
+    oracle at sizes on either side of the bulk-copy kernel's 64-Gaussian tiles (63: the tail kernel
+    only; 200,003: several tiles per persistent block and a tail), with fp32 and fp16 coefficients."""
+    sc = synthetic.clustered_scene(n, seed=9)
+    rt = G.make_tracer(16, 16, sc.mean, sc.rotation, sc.scale, sc.opacity, sh_dc=sc.sh_dc, sh_rest=sc.sh_rest,
+                       sh_degree=0, inference_only=fp16)
+    g = rt.get_gaussians()
+    assert (g.sh_coeffs_rest.dtype == torch.float16) == fp16
+    dc = g.sh_coeffs_dc.float().cpu().numpy().reshape(n, 3)
+    rest = g.sh_coeffs_rest.float().cpu().numpy()
+    _, _, _, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, sc.scale, sc.opacity)
+    want_live = live.copy()
+    want_live[vis == 0, 0] = -np.inf
+    cam = synthetic.orbit_camera(0.7, 16, 16)
+    for deg in range(4):
+        g.current_sh_degree.fill_(deg)
+        g.was_visible.fill_(True)
+        rt.get_camera().vertical_fov_radians.fill_(cam.fov_y)
+        rt.get_camera().set_pose(cam.origin_cuda(), cam.rotation_c2w_blender_cuda())
+        with torch.set_grad_enabled(not fp16):  # an inference tracer keeps no backward hit list
+            rt.forward_pass()
+        torch.cuda.synchronize()
+        rt.check_status()
+        chan = oracle.sh_forward(deg, sc.mean, cam.origin.astype(np.float32), dc, rest)
+        assert np.array_equal(g.channels.cpu().numpy(), chan), deg
+        assert np.array_equal(rt.scene_workspace().live.cpu().numpy(), want_live), deg
+        assert not g.was_visible.any().item(), deg  # set again only by a backward pass
+
+
 def _camera_rays_gpu(rt, cam):
     rt.get_camera().znear.fill_(0.0)
     rt.get_camera().zfar.fill_(99999.9)
