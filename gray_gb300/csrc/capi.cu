@@ -249,6 +249,14 @@ int gray_render_batch(const gray_batch_scene *scenes, const gray_batch_view *vie
     return GRAY_OK;
 }
 
+int gray_selftest_copy_wait(int32_t *status, uint64_t limit_ns, void *stream) {
+    if (!status) return fail(GRAY_ERR_INVALID_ARGUMENT, "selftest_copy_wait: status is NULL");
+    if (limit_ns > 2000000000ull) return fail(GRAY_ERR_OUT_OF_RANGE, "selftest_copy_wait: limit above 2 s");
+    cudaStream_t s = (cudaStream_t)stream;
+    GRAY_LAUNCH("selftest_copy_wait", gray::launch_copy_wait_selftest(status, limit_ns, s));
+    return GRAY_OK;
+}
+
 const char *gray_last_error(void) { return g_last_error.c_str(); }
 
 const char *gray_version(void) { return "gray_gb300 0.1 (sm_103a)"; }

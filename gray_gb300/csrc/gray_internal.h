@@ -17,6 +17,8 @@ cudaError_t launch_snapshot(const gray_params &p, cudaStream_t s);
 // reset_frame: zero was_visible, count the call and empty the backward hit list (forward_pass)
 cudaError_t launch_forward_prep(const gray_params &p, bool reset_frame, cudaStream_t s);
 cudaError_t launch_fold_and_sh_backward(const gray_params &p, cudaStream_t s);
+// a wait on an mbarrier phase that never completes, which must give up and report
+cudaError_t launch_copy_wait_selftest(int32_t *status, uint64_t limit_ns, cudaStream_t s);
 cudaError_t launch_batch_prep(const gray_params &p, const float *origins, int nviews, float *channels_out,
                               cudaStream_t s);
 

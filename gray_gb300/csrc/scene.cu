@@ -313,6 +313,25 @@ cudaError_t launch_snapshot(const gray_params &p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// The bounded wait of the pipelines above, made to run out: 16 bytes are announced on the phase and
+// none are copied, so it never completes.
+__global__ void copy_wait_selftest_kernel(int32_t *status, uint64_t limit_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+        mbar_expect_tx(&bar, 16u);
+    }
+    __syncthreads();
+    if (!__syncthreads_and(mbar_wait(&bar, 0u, limit_ns)) && threadIdx.x == 0)
+        atomicOr(status, GRAY_STATUS_COPY_TIMEOUT);
+}
+
+cudaError_t launch_copy_wait_selftest(int32_t *status, uint64_t limit_ns, cudaStream_t s) {
+    copy_wait_selftest_kernel<<<1, 32, 0, s>>>(status, limit_ns);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------------------------
 // Per-forward preparation: live opacity and scaling factor for the intersection test
 // (cuda/shaders.cu:21-24, 51-53 read them per hit), and the SH colour

@@ -16,7 +16,8 @@
  *  - `stream` is a cudaStream_t passed as void*; 0 selects the legacy default stream.
  *  - Return value: GRAY_OK or a GRAY_ERR_* code; gray_last_error() gives the message.
  *    Conditions that only the device can detect (hit-list overflow, traversal-stack overflow,
- *    an exhausted spin budget) are OR-ed into `*status` (a device int32) instead of trapping;
+ *    an exhausted spin budget, a bulk-copy wait that ran out) are OR-ed into `*status` (a device
+ *    int32) instead of trapping;
  *    the host reads it after synchronising.
  *  - Layouts follow the reference holders (cuda/core/gaussians.h:70-160): mean [N,3],
  *    rotation [N,4] (r,x,y,z, unnormalised), scale [N,3] (log), opacity [N,1] (logit),
@@ -288,6 +289,13 @@ int gray_profiler_collect(char *buf, size_t buflen);
  * rebuild's only. */
 #define GRAY_STATIC_MAX_GAUSSIANS 262144
 int gray_rebuild_bvh_static(const gray_params *p, void *stream);
+
+/* Self-test of the bounded copy wait that the streaming kernels use (no reference counterpart:
+ * failure detection without a GPU fault).  One block announces 16 bytes on an mbarrier phase and
+ * copies nothing, so the phase never completes; the wait gives up after limit_ns nanoseconds
+ * (at most 2 s), sets GRAY_STATUS_COPY_TIMEOUT in *status and the kernel returns.  Nothing else is
+ * read or written. */
+int gray_selftest_copy_wait(int32_t *status, uint64_t limit_ns, void *stream);
 
 /* Message of the last error returned on the calling thread. */
 const char *gray_last_error(void);

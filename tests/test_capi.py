@@ -116,3 +116,14 @@ def test_frontier_and_batch_sizes(gray_lib):
             assert L.gray_batch_groups(w, h, variant) == _ceil(_ceil(w, tw), 2) * _ceil(_ceil(h, th), 2)
             tiles = _ceil(w, 2 * tw) * _ceil(h, 2 * th)  # the forward's block tiles (2x2 packets)
             assert gray_lib.gray_schedule_words(w, h) >= header + tiles * (2 + words), (w, h, variant)
+
+
+def test_copy_wait_selftest_checks_its_arguments(gray_lib):
+    """The copy-wait self-test refuses a NULL status word and a limit above 2 s before any launch."""
+    from gray_gb300 import _lib
+
+    L = _lib.load()
+    L.gray_selftest_copy_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
+    assert L.gray_selftest_copy_wait(None, 1000, None) == 1  # GRAY_ERR_INVALID_ARGUMENT
+    assert b"status" in L.gray_last_error()
+    assert L.gray_selftest_copy_wait(ctypes.c_void_p(16), 3_000_000_000, None) == 3  # GRAY_ERR_OUT_OF_RANGE

@@ -5,6 +5,7 @@ nodes), the fp16-keyed compositing results bit-exact (transmittance T, tail esti
 that depend on the order hits are found in (full transmittance, hence the final colour) within
 float32 rounding, and gradients (float atomics in arbitrary order) within 1e-4 relative.
 """
+import ctypes
 import math
 
 import numpy as np
@@ -416,3 +417,17 @@ def test_trace_variants_are_bit_identical(oracle, variant):
                                bvh=oracle.Bvh(aabb, vis))
     assert fwd["nacc"].max() > 20  # more than one 16-key buffer on some rays
     _compare_forward(rt, fwd)
+
+
+def test_copy_wait_runs_out_reports_and_leaves_the_context_usable(oracle):
+    """A wait on an mbarrier phase that never completes (bytes announced, none copied) gives up after
+    its limit, sets GRAY_STATUS_COPY_TIMEOUT and returns; the context then runs a traced forward
+    that matches the oracle."""
+    L = _lib.load()
+    L.gray_selftest_copy_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    assert L.gray_selftest_copy_wait(status.data_ptr(), 20_000_000, ctypes.c_void_p(stream.cuda_stream)) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 16
+    test_small_scene_sh_camera_and_passes(oracle)
