@@ -2,7 +2,8 @@
 //
 // Each entry point is one method of the reference's torch-bound Raytracer
 // (cuda/raytracer.h:88-149); it validates the caller's state, launches the kernels on the
-// given stream and returns immediately (no host synchronisation, no allocation).
+// given stream and returns immediately (no host synchronisation, no device allocation; the forward
+// entry points make one side stream and two events per host thread and context on first use).
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -88,6 +89,69 @@ ProfScope::~ProfScope() {
 using gray::check_common;
 using gray::cuda_fail;
 
+namespace {
+
+// The calling thread's second stream in one CUDA context, with a fork and a join event; made on first
+// use in that context (highest priority: the forward's tile schedule, which it carries, is on the
+// critical path) and kept until the process exits.
+struct SideStream {
+    unsigned long long ctx;
+    cudaStream_t s;
+    cudaEvent_t fork, join;
+};
+thread_local std::vector<SideStream> t_side;
+
+// false when no side stream can be had (no context id, or a creation failed): run serially
+bool side_stream(SideStream *out) {
+    unsigned long long id = 0;
+    if (!gray::current_context_id(&id)) return false;
+    for (const SideStream &x : t_side)
+        if (x.ctx == id) {
+            *out = x;
+            return true;
+        }
+    SideStream x{id, nullptr, nullptr, nullptr};
+    int lo = 0, hi = 0;
+    bool ok = cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess &&
+              cudaStreamCreateWithPriority(&x.s, cudaStreamNonBlocking, hi) == cudaSuccess &&
+              cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        if (x.fork) cudaEventDestroy(x.fork);
+        if (x.s) cudaStreamDestroy(x.s);
+        cudaGetLastError();  // leave no stale error for the launches that follow
+        return false;
+    }
+    t_side.push_back(x);
+    *out = x;
+    return true;
+}
+
+// forward_prep (live values, colours) and the tile schedule (per-tile BVH frontier and work order,
+// from the BVH and the camera only) read and write disjoint state: the schedule runs on the side
+// stream between a fork and a join event while forward_prep runs on s, and the trace follows both.
+int forward(const gray_params *p, bool display, cudaStream_t s) {
+    SideStream side;
+    const bool overlap = gray::trace_forward_has_schedule(*p) && side_stream(&side);
+    if (overlap) {
+        cudaError_t e;
+        if ((e = cudaEventRecord(side.fork, s)) != cudaSuccess) return cuda_fail(e, "fork");
+        if ((e = cudaStreamWaitEvent(side.s, side.fork, 0)) != cudaSuccess) return cuda_fail(e, "fork");
+        GRAY_LAUNCH_ON("tile_schedule", side.s, gray::launch_trace_schedule(*p, display, side.s));
+        if ((e = cudaEventRecord(side.join, side.s)) != cudaSuccess) return cuda_fail(e, "join");
+    }
+    GRAY_LAUNCH("forward_prep", gray::launch_forward_prep(*p, !display, s));
+    if (overlap) {
+        cudaError_t e = cudaStreamWaitEvent(s, side.join, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "join");
+    }
+    GRAY_LAUNCH("trace_forward", gray::launch_trace_forward(*p, display, overlap, s));
+    GRAY_LAUNCH("ellipsoids", gray::launch_ellipsoids(*p, display, s));
+    return GRAY_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int gray_profiler_enable(int on, int capacity) {
@@ -145,21 +209,13 @@ size_t gray_schedule_words(uint32_t width, uint32_t height) { return gray::gray_
 int gray_forward_pass(const gray_params *p, void *stream) {
     int e = check_trace(p);
     if (e) return e;
-    cudaStream_t s = (cudaStream_t)stream;
-    GRAY_LAUNCH("forward_prep", gray::launch_forward_prep(*p, true, s));
-    GRAY_LAUNCH("trace_forward", gray::launch_trace_forward(*p, false, s));
-    GRAY_LAUNCH("ellipsoids", gray::launch_ellipsoids(*p, false, s));
-    return GRAY_OK;
+    return forward(p, false, (cudaStream_t)stream);
 }
 
 int gray_forward_pass_display(const gray_params *p, void *stream) {
     int e = check_trace(p);
     if (e) return e;
-    cudaStream_t s = (cudaStream_t)stream;
-    GRAY_LAUNCH("forward_prep", gray::launch_forward_prep(*p, false, s));
-    GRAY_LAUNCH("trace_forward", gray::launch_trace_forward(*p, true, s));
-    GRAY_LAUNCH("ellipsoids", gray::launch_ellipsoids(*p, true, s));
-    return GRAY_OK;
+    return forward(p, true, (cudaStream_t)stream);
 }
 
 int gray_backward_pass(const gray_params *p, void *stream) {

@@ -37,7 +37,12 @@ constexpr size_t sort_tmp_words(int n) {
 
 // trace.cu
 // display: forward_pass_display (colour only; no hit lists or saved state, whatever grads_enabled holds)
-cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_t s);
+// the forward's tile schedule (per-tile work estimate and BVH frontier, densest-first order); it
+// reads only the BVH and the camera, so it may run on another stream than forward_prep
+bool trace_forward_has_schedule(const gray_params &p);
+cudaError_t launch_trace_schedule(const gray_params &p, bool display, cudaStream_t s);
+// schedule_ready: launch_trace_schedule has been issued for this forward (and ordered before s)
+cudaError_t launch_trace_forward(const gray_params &p, bool display, bool schedule_ready, cudaStream_t s);
 size_t gray_schedule_words_for(uint32_t width, uint32_t height);
 // ellipsoid view; a no-op launch unless config.render_ellipsoids is set
 cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s);
@@ -68,17 +73,22 @@ class ProfScope {
     cudaStream_t s_;
 };
 
-// Run one launcher inside a profiler scope; return its error from the enclosing entry point.
-// Needs a cudaStream_t named `s` in scope.
-#define GRAY_LAUNCH(name, expr)                                            \
+// Run one launcher inside a profiler scope on stream `strm`; return its error from the enclosing
+// entry point.  GRAY_LAUNCH uses the cudaStream_t named `s` in scope.
+#define GRAY_LAUNCH_ON(name, strm, expr)                                   \
     do {                                                                   \
         cudaError_t _e;                                                    \
         {                                                                  \
-            ::gray::ProfScope _ps(name, s);                                \
+            ::gray::ProfScope _ps(name, strm);                             \
             _e = (expr);                                                   \
         }                                                                  \
         if (_e != cudaSuccess) return ::gray::cuda_fail(_e, name);         \
     } while (0)
+#define GRAY_LAUNCH(name, expr) GRAY_LAUNCH_ON(name, s, expr)
+
+// noalloc.cu: unique id of the calling thread's current CUDA context (false when the driver
+// cannot tell, or no context is current)
+bool current_context_id(unsigned long long *id);
 
 constexpr int kThreads = 256;
 inline unsigned int blocks_for(long long n, int threads = kThreads) {

@@ -44,7 +44,7 @@ struct CachedScratch {
 
 std::mutex g_mu;
 std::vector<CachedScratch> g_cache;
-bool g_driver_resolved = false;
+std::once_flag g_driver_resolved;
 CtxGetCurrentFn g_ctx_get_current = nullptr;
 CtxGetIdFn g_ctx_get_id = nullptr;
 
@@ -53,9 +53,7 @@ int fail(int code, const std::string &what) {
     return code;
 }
 
-void resolve_driver_entry_points() {
-    if (g_driver_resolved) return;
-    g_driver_resolved = true;
+void resolve_driver_entry_points_once() {
     void *fn = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
@@ -67,16 +65,13 @@ void resolve_driver_entry_points() {
         g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(fn);
 }
 
+void resolve_driver_entry_points() { std::call_once(g_driver_resolved, resolve_driver_entry_points_once); }
+
 // Device address of g_static_scratch in the calling thread's current context.
 int scratch_address(uint32_t **out) {
     std::lock_guard<std::mutex> lock(g_mu);
-    resolve_driver_entry_points();
     unsigned long long id = 0;
-    bool have_id = false;
-    if (g_ctx_get_current && g_ctx_get_id) {
-        CUcontext ctx = nullptr;
-        if (g_ctx_get_current(&ctx) == CUDA_SUCCESS && ctx && g_ctx_get_id(ctx, &id) == CUDA_SUCCESS) have_id = true;
-    }
+    bool have_id = gray::current_context_id(&id);
     if (have_id)
         for (const CachedScratch &c : g_cache)
             if (c.ctx_id == id) {
@@ -89,15 +84,23 @@ int scratch_address(uint32_t **out) {
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_scratch);
     if (e != cudaSuccess) return fail(GRAY_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     *out = static_cast<uint32_t *>(ptr);
-    if (!have_id && g_ctx_get_current && g_ctx_get_id) {
-        CUcontext ctx = nullptr;
-        if (g_ctx_get_current(&ctx) == CUDA_SUCCESS && ctx && g_ctx_get_id(ctx, &id) == CUDA_SUCCESS) have_id = true;
-    }
+    if (!have_id) have_id = gray::current_context_id(&id);
     if (have_id) g_cache.push_back(CachedScratch{id, *out});  // without context ids: look up on every call
     return GRAY_OK;
 }
 
 }  // namespace
+
+namespace gray {
+
+bool current_context_id(unsigned long long *id) {
+    resolve_driver_entry_points();
+    if (!g_ctx_get_current || !g_ctx_get_id) return false;
+    CUcontext ctx = nullptr;
+    return g_ctx_get_current(&ctx) == CUDA_SUCCESS && ctx && g_ctx_get_id(ctx, id) == CUDA_SUCCESS;
+}
+
+}  // namespace gray
 
 extern "C" {
 

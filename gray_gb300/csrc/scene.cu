@@ -430,6 +430,7 @@ __global__ void __launch_bounds__(kPrepThreads) forward_prep_kernel(
 // two stages, then the output copy (colours 12T, live 8T, flags T).
 constexpr int kPrepTile = 64;
 static_assert(kPrepTile % 16 == 0, "every per-tile range must span a multiple of 16 bytes");
+constexpr int kPrepBlocksPerSm = 4;
 
 __host__ __device__ __forceinline__ uint32_t prep_stage_bytes(int num_rest, uint32_t sb) {
     return 17u * kPrepTile + 3u * kPrepTile * sb + (uint32_t)kPrepTile * 3u * (uint32_t)num_rest * sb;
@@ -567,7 +568,9 @@ static cudaError_t forward_prep_typed(const gray_params &p, bool reset_frame, cu
         if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forward_prep_bulk_kernel<SHT>, kPrepTile,
                                                                smem)) != cudaSuccess)
             return e;
-        const int want = sms * (per_sm > 0 ? per_sm : 1);
+        // at most kPrepBlocksPerSm blocks per SM: the forward's tile schedule runs beside this kernel
+        // on another stream, and its blocks need shared memory too
+        const int want = sms * min(per_sm > 0 ? per_sm : 1, kPrepBlocksPerSm);
         forward_prep_bulk_kernel<SHT><<<tiles < want ? tiles : want, kPrepTile, smem, s>>>(
             tiles, num_rest, g.opacity, p.scene.visible, p.config.alpha_threshold, p.config.exp_power,
             p.config.enable_sh, g.current_sh_degree, g.max_sh_degree, g.mean, p.camera.origin, dc, rest, g.channels,

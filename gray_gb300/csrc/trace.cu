@@ -1558,8 +1558,20 @@ cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s
     return cudaGetLastError();
 }
 
-cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_t s) {
-    FwdArgs a = forward_args(p, display);
+// Launch shape of one forward: the kernel arguments, the trace kernel and its grid, and whether the
+// tile schedule (work estimate, densest-first order, per-tile BVH frontier) is used.
+struct FwdPlan {
+    FwdArgs a;
+    const void *kern;
+    dim3 grid;
+    int bw, bh;
+    bool sched;
+};
+
+static FwdPlan plan_forward(const gray_params &p, bool display) {
+    FwdPlan q;
+    FwdArgs &a = q.a;
+    a = forward_args(p, display);
     // variant: bits 0-1 select (buffer size, register cap), bit 2 the packet shape, bits 3-4 the
     // tile frontier's cut (64 leaves, 32, 128, no frontier), bit 5 packets claimed per warp
     // (trace_forward_claim_kernel) instead of tiles per block
@@ -1568,46 +1580,65 @@ cudaError_t launch_trace_forward(const gray_params &p, bool display, cudaStream_
     const bool claim = (v & 32) != 0;
     a.tile_w = (v & 4) ? 4 : 8;
     a.tile_h = 32 / a.tile_w;
-    const int bw = a.tile_w * kBlockWarpsX, bh = a.tile_h * kBlockWarpsY;
-    dim3 grid((p.render_width + bw - 1) / bw, (p.render_height + bh - 1) / bh);
-    a.tiles_x = (int)grid.x;
-    a.ntiles = (int)(grid.x * grid.y);
+    q.bw = a.tile_w * kBlockWarpsX;
+    q.bh = a.tile_h * kBlockWarpsY;
+    q.grid = dim3((p.render_width + q.bw - 1) / q.bw, (p.render_height + q.bh - 1) / q.bh);
+    a.tiles_x = (int)q.grid.x;
+    a.ntiles = (int)(q.grid.x * q.grid.y);
     a.schedule = nullptr;
-    const void *kern;
     const size_t words = gray_schedule_words_for(p.image_width, p.image_height);
-    const bool sched = p.hitlist.schedule && a.ntiles > 0 && (size_t)a.ntiles <= (words - kSchedHeader) / 2;
+    q.sched = p.hitlist.schedule && a.ntiles > 0 && (size_t)a.ntiles <= (words - kSchedHeader) / 2;
 #define GRAY_FWD_KERNEL(KB, MINB)                                                                   \
-    (!sched ? reinterpret_cast<const void *>(&trace_forward_kernel<KB, MINB>)                       \
-     : claim ? reinterpret_cast<const void *>(&trace_forward_claim_kernel<KB, MINB>)                \
-             : reinterpret_cast<const void *>(&trace_forward_sched_kernel<KB, MINB>))
+    (!q.sched ? reinterpret_cast<const void *>(&trace_forward_kernel<KB, MINB>)                     \
+     : claim  ? reinterpret_cast<const void *>(&trace_forward_claim_kernel<KB, MINB>)               \
+              : reinterpret_cast<const void *>(&trace_forward_sched_kernel<KB, MINB>))
     switch (v & 3) {
-        case 0: kern = GRAY_FWD_KERNEL(32, 1); break;
-        case 1: kern = GRAY_FWD_KERNEL(32, 4); break;
-        case 2: kern = GRAY_FWD_KERNEL(16, 1); break;
-        default: kern = GRAY_FWD_KERNEL(16, 6); break;
+        case 0: q.kern = GRAY_FWD_KERNEL(32, 1); break;
+        case 1: q.kern = GRAY_FWD_KERNEL(32, 4); break;
+        case 2: q.kern = GRAY_FWD_KERNEL(16, 1); break;
+        default: q.kern = GRAY_FWD_KERNEL(16, 6); break;
     }
 #undef GRAY_FWD_KERNEL
-    cudaError_t e;
-    if (sched) {
-        // densest tiles first: estimate, bucket, then a persistent grid that takes tiles in order
+    if (q.sched) {
         a.schedule = p.hitlist.schedule;
         a.frontier_cut = fcut == 0 ? kFrontierCutDefault : fcut == 1 ? 32u : fcut == 2 ? 128u : 0u;
         if (a.frontier_cut > 0 && (size_t)a.ntiles <= (words - kSchedHeader) / (2 + kFrontierWords))
             a.frontier = a.schedule + kSchedHeader + 2 * (size_t)a.ntiles;
-        if ((e = cudaMemsetAsync(a.schedule, 0, sizeof(uint32_t) * kSchedHeader, s)) != cudaSuccess) return e;
-        tile_cost_kernel<<<a.ntiles, 32, 0, s>>>(a, bw, bh);
-        sched_scan_kernel<<<1, 32, 0, s>>>(a.schedule);
-        sched_scatter_kernel<<<(a.ntiles + 255) / 256, 256, 0, s>>>(a.schedule, a.ntiles);
+    }
+    return q;
+}
+
+bool trace_forward_has_schedule(const gray_params &p) { return plan_forward(p, false).sched; }
+
+cudaError_t launch_trace_schedule(const gray_params &p, bool display, cudaStream_t s) {
+    const FwdPlan q = plan_forward(p, display);
+    if (!q.sched) return cudaSuccess;
+    // densest tiles first: per-tile estimate and frontier, bucket by log2 of the estimate, order
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(q.a.schedule, 0, sizeof(uint32_t) * kSchedHeader, s)) != cudaSuccess) return e;
+    tile_cost_kernel<<<q.a.ntiles, 32, 0, s>>>(q.a, q.bw, q.bh);
+    sched_scan_kernel<<<1, 32, 0, s>>>(q.a.schedule);
+    sched_scatter_kernel<<<(q.a.ntiles + 255) / 256, 256, 0, s>>>(q.a.schedule, q.a.ntiles);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_forward(const gray_params &p, bool display, bool schedule_ready, cudaStream_t s) {
+    FwdPlan q = plan_forward(p, display);
+    cudaError_t e;
+    dim3 grid = q.grid;
+    if (q.sched) {
+        if (!schedule_ready && (e = launch_trace_schedule(p, display, s)) != cudaSuccess) return e;
+        // a persistent grid that takes the tiles in the schedule's order
         int dev = 0, sms = 0, per_sm = 0;
         if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
         if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFwdThreads, 0)) != cudaSuccess)
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, q.kern, kFwdThreads, 0)) != cudaSuccess)
             return e;
         const unsigned int want = (unsigned int)(sms * (per_sm > 0 ? per_sm : 1));
-        grid = dim3(want < (unsigned int)a.ntiles ? want : (unsigned int)a.ntiles, 1, 1);
+        grid = dim3(want < (unsigned int)q.a.ntiles ? want : (unsigned int)q.a.ntiles, 1, 1);
     }
-    void *args[] = {&a};
-    if ((e = cudaLaunchKernel(kern, grid, dim3(kFwdThreads), args, 0, s)) != cudaSuccess) return e;
+    void *args[] = {&q.a};
+    if ((e = cudaLaunchKernel(q.kern, grid, dim3(kFwdThreads), args, 0, s)) != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
