@@ -1944,12 +1944,16 @@ __device__ __forceinline__ void replay_hit(const BwdArgs &a, const BwdPixel &px,
     const float gv = eval_gaussian(sq, px.pw);
     const float alpha = maxalpha_mul(gv, o);
 
+    // one reciprocal of (1 - alpha) instead of four divisions (the reference divides each time,
+    // cuda/backward_pass.cu:51-59,141); the gradients differ from it by rounding only
     const float om = 1.0f - alpha;
-    const float w = T / om * alpha;
+    const float rom = 1.0f / om;
+    const float Tr = T * rom;
+    const float w = Tr * alpha;
     const float dgc = dot3(px.gout, c);
-    float ga = (dgc - gT) * T / om;
-    ga = ga + -px.fT / om * px.dbg;
-    ga = ga + -((px.Tfin - px.fT) / om) * px.drem;
+    float ga = (dgc - gT) * Tr;
+    ga = ga + -(px.fT * rom) * px.dbg;
+    ga = ga + -((px.Tfin - px.fT) * rom) * px.drem;
     gT = gT + (dgc - gT) * alpha;
     float go = maxalpha_mul(ga, gv);
     go = go * o * (1.0f - o);
@@ -1988,7 +1992,7 @@ __device__ __forceinline__ void replay_hit(const BwdArgs &a, const BwdPixel &px,
                    -gxw.x, -gxw.y, -gxw.z, go, gs.x, gs.y, gs.z, w * px.inv_npix,
                    px.gout.x * w, px.gout.y * w, px.gout.z * w, 1.0f};
     reduce_hit(a.grad_acc + 16 * (size_t)gid, gid, v);
-    T = T / om;
+    T = Tr;
 }
 
 // One thread per pixel walks its composited hits back to front (16x8-pixel blocks of four 8x4-pixel

@@ -176,6 +176,42 @@ def test_forward_prep_tiles_bit_exact(oracle, n, fp16):
         assert not g.was_visible.any().item(), deg  # set again only by a backward pass
 
 
+def test_forward_captured_in_a_cuda_graph_matches_eager(oracle):
+    """A forward captured in a CUDA graph (the tile schedule on the library's side stream, forked from
+    and joined back to the capturing stream) replays to the same image, transmittances and hit lists
+    as the eager call, which match the oracle."""
+    sc = synthetic.small_scene(seed=4, n=300)
+    cam = synthetic.camera_small(64, 64, 64.0)
+    rt = G.make_tracer(64, 64, sc.mean, sc.rotation, sc.scale, sc.opacity, sh_dc=sc.sh_dc, sh_rest=sc.sh_rest,
+                       sh_degree=3)
+    ro, rd = _camera_rays_gpu(rt, cam)  # eager forward (with gradients: hit lists recorded)
+    eager = G.fb_numpy(rt)
+    eager_lists = G.hit_lists(rt)
+    chan = oracle.sh_forward(3, sc.mean, cam.origin.astype(np.float32), sc.sh_dc[:, 0, :], sc.sh_rest)
+    geom, l2w, aabb, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, sc.scale, sc.opacity)
+    fwd = oracle.trace_forward(ro, rd, geom, live, chan, vis, oracle.TraceConfig(t_threshold=0.03))
+    _compare_forward(rt, fwd)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side), torch.enable_grad():
+        rt.forward_pass()  # warm-up on the capturing stream's thread and context
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g), torch.enable_grad():
+        rt.forward_pass()
+    fb = rt.get_framebuffer()
+    for k in ("output_channels", "transmittance", "full_transmittance"):
+        getattr(fb, k).fill_(-1.0)
+    g.replay()
+    torch.cuda.synchronize()
+    rt.check_status()
+    replayed = G.fb_numpy(rt)
+    for k in ("output_channels", "transmittance", "full_transmittance", "remaining_channels_estimate"):
+        assert np.array_equal(replayed[k], eager[k]), k
+    assert all(np.array_equal(a, b) for a, b in zip(G.hit_lists(rt), eager_lists))
+
+
 def _camera_rays_gpu(rt, cam):
     rt.get_camera().znear.fill_(0.0)
     rt.get_camera().zfar.fill_(99999.9)
