@@ -65,6 +65,8 @@ struct FwdArgs {
     int tiles_x, ntiles;
     uint32_t *frontier;  // per-tile BVH frontiers (null: packets start at the root)
     uint32_t frontier_cut;
+    uint32_t *super_frontier;  // per super-tile coarse frontiers seeding the tile walks (null: root)
+    int super_x;               // super-tiles per row
     const uint32_t *total_num_calls;
     const float4 *geom, *l2w;
     const float2 *live;
@@ -992,12 +994,23 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_claim_kernel(
 // frontier: every ray of the tile that hits a Gaussian reaches it through one of them, so the tile's
 // packets start their traversals there instead of at the root (the top levels are walked once per
 // tile, not once per packet traversal).  The frontier is sorted by its boxes' centres along the
-// tile's mean direction, so packets visit it roughly front to back.  Schedule words: [0] work
-// counter, [1..33] bucket counts/cursors, [kSchedHeader, +ntiles) estimates, [kSchedHeader + ntiles,
-// +ntiles) order, then (when frontiers are on) kFrontierWords words per tile.
+// tile's mean direction, so packets visit it roughly front to back.  The tiles' walks share their
+// top: a first pass walks each super-tile (kSuperTiles x kSuperTiles tiles) down to nodes of at
+// most kSuperCut leaves and stores them with their boxes; a tile's walk then starts from its
+// super-tile's entries, testing each entry's own box against the tile's frustum, instead of from the
+// root.  Every leaf a ray of the tile can hit lies under an entry of the super-tile (its ancestors
+// meet the tile's frustum, hence the super-tile's), so the tile still reaches it.  Schedule words:
+// [0] work counter, [1..33] bucket counts/cursors, [kSchedHeader, +ntiles) estimates, [kSchedHeader +
+// ntiles, +ntiles) order, then (when frontiers are on) kFrontierWords words per tile, then
+// kSuperWords words per super-tile.
 // ---------------------------------------------------------------------------------------------
 constexpr int kCostCut = 512;
 constexpr int kCostStack = 256;
+constexpr int kSuperTiles = 4;
+constexpr uint32_t kSuperCut = 1024;
+constexpr int kSuperMax = 255;          // entries of a super-tile frontier (fits the walk's buffer)
+constexpr int kSuperEntryWords = 8;     // link, leaves below, box min xyz, box max xyz
+constexpr int kSuperWords = 1 + kSuperMax * kSuperEntryWords;
 
 struct FrontierScratch {
     Frustum fr;
@@ -1006,22 +1019,82 @@ struct FrontierScratch {
     uint32_t val[kFrontierSort];
 };
 
+// What the super-tile walk also keeps of each frontier entry.
+struct SuperScratch {
+    float box[kFrontierSort][6];
+    uint32_t leaves[kFrontierSort];
+};
+
 // One warp walks the top of the BVH for a pixel rectangle whose frustum is in fs.fr: returns (on
 // every lane) the number of leaves under the frontier, the nodes of at most `cut` leaves (and the
 // leaves) it reaches; with `out`, writes the frontier there sorted front to back (count + entries),
 // or a count of kFrontierNone when the walk was cut short, the frontier does not fit or the tree is
-// malformed.  n > 1.
+// malformed.  n > 1.  seed (may be null; a count above kSuperMax means none): a super-tile frontier
+// to start from instead of the root -- each entry whose box meets this frustum is walked further
+// (more than `cut` leaves) or is a frontier entry.  SUPER: the walk of a super-tile; with `out` it
+// writes its entries unsorted with their leaf counts and boxes (kSuperWords words), or
+// kFrontierNone when they do not fit.
+template <bool SUPER>
 __device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, uint32_t cut, FrontierScratch &fs,
-                                               uint32_t *out) {
+                                               SuperScratch *ss, uint32_t *out, const uint32_t *seed) {
     const int lane = threadIdx.x & 31;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     const Frustum &fr = fs.fr;
+    const float4 cdir = fr.pn[4];  // the near plane's normal: the rectangle's mean direction
     uint32_t est = 0;
-    int nf = 0, sp = 1;
-    bool complete = true;
-    if (lane == 0) fs.stk[0] = 0u;
+    int nf = 0, sp = 0;
+    bool complete = true, stop = false;
+    const uint32_t nseed = seed ? seed[0] : kFrontierNone;
+    if (nseed <= (uint32_t)kSuperMax) {
+        for (int b0 = 0; b0 < (int)nseed; b0 += 32) {
+            const int i = b0 + lane;
+            bool push = false, rec = false, bad = false;
+            uint32_t link = 0;
+            float key = 0.0f;
+            if (i < (int)nseed) {
+                const uint32_t *e = seed + 1 + (size_t)i * kSuperEntryWords;
+                link = e[0];
+                const uint32_t lv = e[1];
+                const float bmin[3] = {__uint_as_float(e[2]), __uint_as_float(e[3]), __uint_as_float(e[4])};
+                const float bmax[3] = {__uint_as_float(e[5]), __uint_as_float(e[6]), __uint_as_float(e[7])};
+                if (frustum_box(fr, bmin, bmax)) {
+                    if (link & GRAY_LEAF_BIT) {
+                        rec = (link & ~GRAY_LEAF_BIT) < (uint32_t)n;
+                        bad = !rec;
+                        est += rec ? 1u : 0u;
+                    } else if (link < (uint32_t)(n - 1)) {
+                        push = lv > cut;
+                        rec = !push;
+                        if (rec) est += lv;
+                    } else {
+                        bad = true;
+                    }
+                    key = fmaf(bmin[2] + bmax[2], cdir.z, fmaf(bmin[1] + bmax[1], cdir.y, (bmin[0] + bmax[0]) * cdir.x));
+                }
+            }
+            if (__any_sync(kFull, bad)) complete = false;
+            const uint32_t mp = __ballot_sync(kFull, push);
+            if (sp + __popc(mp) > kCostStack) {
+                complete = false;  // an estimate from what was reached is enough
+                stop = true;
+                break;
+            }
+            if (push) fs.stk[sp + __popc(mp & lanemask_lt)] = link;
+            sp += __popc(mp);
+            const uint32_t mr = __ballot_sync(kFull, rec);
+            const int at = nf + __popc(mr & lanemask_lt);
+            if (rec && at < kFrontierSort) {
+                fs.key[at] = key;
+                fs.val[at] = link;
+            }
+            nf += __popc(mr);
+        }
+    } else {
+        if (lane == 0) fs.stk[0] = 0u;
+        sp = 1;
+    }
     __syncwarp();
-    for (int guard = 0; sp > 0; guard++) {
+    for (int guard = 0; sp > 0 && !stop; guard++) {
         if (guard >= 4096) {
             complete = false;
             break;
@@ -1035,6 +1108,7 @@ __device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, ui
         uint32_t ca = 0, cb = 0, la = 0, lb = 0;  // children and the leaves below them
         bool pa = false, pb = false, bad = false;
         float sa = 0.0f, sb = 0.0f;
+        float boxa[6], boxb[6];
         if (node != GRAY_NULL) {
             if (node >= (uint32_t)(n - 1)) {
                 bad = true;
@@ -1046,9 +1120,8 @@ __device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, ui
                 const uint32_t c0 = __float_as_uint(q3.x), c1 = __float_as_uint(q3.y);
                 const uint32_t l0 = __float_as_uint(q3.w), l1 = __float_as_uint(q3.z) - l0;
                 const bool p0 = frustum_box(fr, b0min, b0max), p1 = frustum_box(fr, b1min, b1max);
-                const float4 c = fr.pn[4];
-                const float s0 = fmaf(q0.z + q1.y, c.z, fmaf(q0.y + q1.x, c.y, (q0.x + q0.w) * c.x));
-                const float s1 = fmaf(q2.x + q2.w, c.z, fmaf(q1.w + q2.z, c.y, (q1.z + q2.y) * c.x));
+                const float s0 = fmaf(q0.z + q1.y, cdir.z, fmaf(q0.y + q1.x, cdir.y, (q0.x + q0.w) * cdir.x));
+                const float s1 = fmaf(q2.x + q2.w, cdir.z, fmaf(q1.w + q2.z, cdir.y, (q1.z + q2.y) * cdir.x));
                 const bool sw = s1 < s0;
                 ca = sw ? c1 : c0;
                 cb = sw ? c0 : c1;
@@ -1058,6 +1131,15 @@ __device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, ui
                 sb = sw ? s0 : s1;
                 la = sw ? l1 : l0;
                 lb = sw ? l0 : l1;
+                if constexpr (SUPER) {
+                    const float c0b[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+                    const float c1b[6] = {q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+#pragma unroll
+                    for (int k = 0; k < 6; k++) {
+                        boxa[k] = sw ? c1b[k] : c0b[k];
+                        boxb[k] = sw ? c0b[k] : c1b[k];
+                    }
+                }
             }
         }
         // internal children above the cut are walked further; leaves and nodes at the cut are
@@ -1106,52 +1188,97 @@ __device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, ui
         if (fa && before < kFrontierSort) {
             fs.key[before] = sa;
             fs.val[before] = ca;
+            if constexpr (SUPER) {
+                ss->leaves[before] = (ca & GRAY_LEAF_BIT) ? 1u : la;
+#pragma unroll
+                for (int k = 0; k < 6; k++) ss->box[before][k] = boxa[k];
+            }
         }
-        if (fb && before + (fa ? 1 : 0) < kFrontierSort) {
-            fs.key[before + (fa ? 1 : 0)] = sb;
-            fs.val[before + (fa ? 1 : 0)] = cb;
+        const int bb = before + (fa ? 1 : 0);
+        if (fb && bb < kFrontierSort) {
+            fs.key[bb] = sb;
+            fs.val[bb] = cb;
+            if constexpr (SUPER) {
+                ss->leaves[bb] = (cb & GRAY_LEAF_BIT) ? 1u : lb;
+#pragma unroll
+                for (int k = 0; k < 6; k++) ss->box[bb][k] = boxb[k];
+            }
         }
         nf += __popc(qa) + __popc(qb);
         __syncwarp();
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) est += __shfl_xor_sync(kFull, est, off);
-    if (out) {
-        if (complete && nf <= kFrontierMax) {
-            // bitonic sort of the entries by key (padding sorts last); NaN keys compare false
-            int p2 = 32;
-            while (p2 < nf) p2 <<= 1;
-            for (int i = nf + lane; i < p2; i += 32) {
-                fs.key[i] = __int_as_float(0x7f800000);
-                fs.val[i] = GRAY_NULL;
+    if (!out) return est;
+    if constexpr (SUPER) {
+        if (complete && nf <= kSuperMax) {
+            for (int i = lane; i < nf; i += 32) {
+                uint32_t *e = out + 1 + (size_t)i * kSuperEntryWords;
+                e[0] = fs.val[i];
+                e[1] = ss->leaves[i];
+#pragma unroll
+                for (int k = 0; k < 6; k++) e[2 + k] = __float_as_uint(ss->box[i][k]);
             }
-            __syncwarp();
-            for (int k = 2; k <= p2; k <<= 1) {
-                for (int j = k >> 1; j > 0; j >>= 1) {
-                    for (int i = lane; i < p2; i += 32) {
-                        const int ixj = i ^ j;
-                        if (ixj > i) {
-                            const float ki = fs.key[i], kj = fs.key[ixj];
-                            const bool up = (i & k) == 0;
-                            if (up ? (kj < ki) : (ki < kj)) {
-                                fs.key[i] = kj;
-                                fs.key[ixj] = ki;
-                                const uint32_t v = fs.val[i];
-                                fs.val[i] = fs.val[ixj];
-                                fs.val[ixj] = v;
-                            }
-                        }
-                    }
-                    __syncwarp();
-                }
-            }
-            for (int i = lane; i < nf; i += 32) out[1 + i] = fs.val[i];
             if (lane == 0) out[0] = (uint32_t)nf;
         } else if (lane == 0) {
             out[0] = kFrontierNone;
         }
+        return est;
+    }
+    if (complete && nf <= kFrontierMax) {
+        // bitonic sort of the entries by key (padding sorts last); NaN keys compare false
+        int p2 = 32;
+        while (p2 < nf) p2 <<= 1;
+        for (int i = nf + lane; i < p2; i += 32) {
+            fs.key[i] = __int_as_float(0x7f800000);
+            fs.val[i] = GRAY_NULL;
+        }
+        __syncwarp();
+        for (int k = 2; k <= p2; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = lane; i < p2; i += 32) {
+                    const int ixj = i ^ j;
+                    if (ixj > i) {
+                        const float ki = fs.key[i], kj = fs.key[ixj];
+                        const bool up = (i & k) == 0;
+                        if (up ? (kj < ki) : (ki < kj)) {
+                            fs.key[i] = kj;
+                            fs.key[ixj] = ki;
+                            const uint32_t v = fs.val[i];
+                            fs.val[i] = fs.val[ixj];
+                            fs.val[ixj] = v;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        for (int i = lane; i < nf; i += 32) out[1 + i] = fs.val[i];
+        if (lane == 0) out[0] = (uint32_t)nf;
+    } else if (lane == 0) {
+        out[0] = kFrontierNone;
     }
     return est;
+}
+
+// Coarse frontiers of the super-tiles (kSuperTiles x kSuperTiles block tiles each), one warp each.
+__global__ void __launch_bounds__(32) super_cost_kernel(const FwdArgs a, int bw, int bh, int nsuper) {
+    __shared__ FrontierScratch fs;
+    __shared__ SuperScratch ss;
+    const int st = blockIdx.x, lane = threadIdx.x;
+    if (st >= nsuper) return;
+    uint32_t *out = a.super_frontier + (size_t)st * kSuperWords;
+    const int n = a.n;
+    if (!*a.rays_from_python && !*a.jitter && !*a.render_ellipsoids && n > 1) {
+        const int x0 = (st % a.super_x) * kSuperTiles * bw, y0 = (st / a.super_x) * kSuperTiles * bh;
+        const int x1 = min(x0 + kSuperTiles * bw, (int)a.render_w) - 1;
+        const int y1 = min(y0 + kSuperTiles * bh, (int)a.render_h) - 1;
+        make_frustum_warp(fs.fr, mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]), a.w2c, *a.fov, x0, y0, x1, y1,
+                          a.render_w, a.render_h, a.root_box);
+        frontier_walk<true>(a.nodes, n, kSuperCut, fs, &ss, out, nullptr);
+    } else if (lane == 0) {
+        out[0] = kFrontierNone;
+    }
 }
 
 __global__ void __launch_bounds__(32) tile_cost_kernel(const FwdArgs a, int bw, int bh) {
@@ -1165,7 +1292,13 @@ __global__ void __launch_bounds__(32) tile_cost_kernel(const FwdArgs a, int bw, 
         const int x1 = min(x0 + bw, (int)a.render_w) - 1, y1 = min(y0 + bh, (int)a.render_h) - 1;
         make_frustum_warp(fs.fr, mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]), a.w2c, *a.fov, x0, y0, x1, y1,
                           a.render_w, a.render_h, a.root_box);
-        est = frontier_walk(a.nodes, n, a.frontier_cut > 0 ? a.frontier_cut : (uint32_t)kCostCut, fs, out);
+        const uint32_t *seed = nullptr;
+        if (a.super_frontier) {
+            const int sx = (tile % a.tiles_x) / kSuperTiles, sy = (tile / a.tiles_x) / kSuperTiles;
+            seed = a.super_frontier + (size_t)(sy * a.super_x + sx) * kSuperWords;
+        }
+        est = frontier_walk<false>(a.nodes, n, a.frontier_cut > 0 ? a.frontier_cut : (uint32_t)kCostCut, fs, nullptr,
+                                   out, seed);
     } else if (out && lane == 0) {
         out[0] = kFrontierNone;
     }
@@ -1411,7 +1544,7 @@ __global__ void __launch_bounds__(32) batch_frontier_kernel(const gray_batch_sce
     const int x1 = min(x0 + 2 * tile_w, (int)vw.width) - 1, y1 = min(y0 + 2 * tile_h, (int)vw.height) - 1;
     make_frustum_warp(fs.fr, mk3(vw.origin[0], vw.origin[1], vw.origin[2]), vw.w2c, vw.fov_y, x0, y0, x1, y1, vw.width,
                       vw.height, bs.root_box);
-    frontier_walk(reinterpret_cast<const float4 *>(bs.nodes), bs.n, cut, fs, out);
+    frontier_walk<false>(reinterpret_cast<const float4 *>(bs.nodes), bs.n, cut, fs, nullptr, out, nullptr);
 }
 
 template <int KB, int MINB>
@@ -1541,6 +1674,8 @@ static FwdArgs forward_args(const gray_params &p, bool display) {
     a.schedule = nullptr;
     a.frontier = nullptr;
     a.frontier_cut = 0;
+    a.super_frontier = nullptr;
+    a.super_x = 0;
     return a;
 }
 
@@ -1566,10 +1701,12 @@ struct FwdPlan {
     dim3 grid;
     int bw, bh;
     bool sched;
+    int nsuper;  // super-tiles whose coarse frontiers seed the tile walks (0: tiles walk from the root)
 };
 
 static FwdPlan plan_forward(const gray_params &p, bool display) {
     FwdPlan q;
+    q.nsuper = 0;
     FwdArgs &a = q.a;
     a = forward_args(p, display);
     // variant: bits 0-1 select (buffer size, register cap), bit 2 the packet shape, bits 3-4 the
@@ -1604,6 +1741,17 @@ static FwdPlan plan_forward(const gray_params &p, bool display) {
         a.frontier_cut = fcut == 0 ? kFrontierCutDefault : fcut == 1 ? 32u : fcut == 2 ? 128u : 0u;
         if (a.frontier_cut > 0 && (size_t)a.ntiles <= (words - kSchedHeader) / (2 + kFrontierWords))
             a.frontier = a.schedule + kSchedHeader + 2 * (size_t)a.ntiles;
+        if (a.frontier) {
+            // super-tiles after the tiles' frontiers, when the buffer holds them
+            const int sx = (a.tiles_x + kSuperTiles - 1) / kSuperTiles;
+            const int sy = ((int)q.grid.y + kSuperTiles - 1) / kSuperTiles;
+            const size_t used = (size_t)kSchedHeader + (2 + (size_t)kFrontierWords) * (size_t)a.ntiles;
+            if (used + (size_t)sx * (size_t)sy * kSuperWords <= words) {
+                a.super_frontier = a.frontier + (size_t)a.ntiles * kFrontierWords;
+                a.super_x = sx;
+                q.nsuper = sx * sy;
+            }
+        }
     }
     return q;
 }
@@ -1616,6 +1764,7 @@ cudaError_t launch_trace_schedule(const gray_params &p, bool display, cudaStream
     // densest tiles first: per-tile estimate and frontier, bucket by log2 of the estimate, order
     cudaError_t e;
     if ((e = cudaMemsetAsync(q.a.schedule, 0, sizeof(uint32_t) * kSchedHeader, s)) != cudaSuccess) return e;
+    if (q.nsuper > 0) super_cost_kernel<<<q.nsuper, 32, 0, s>>>(q.a, q.bw, q.bh, q.nsuper);
     tile_cost_kernel<<<q.a.ntiles, 32, 0, s>>>(q.a, q.bw, q.bh);
     sched_scan_kernel<<<1, 32, 0, s>>>(q.a.schedule);
     sched_scatter_kernel<<<(q.a.ntiles + 255) / 256, 256, 0, s>>>(q.a.schedule, q.a.ntiles);
@@ -1648,7 +1797,11 @@ size_t gray_schedule_words_for(uint32_t width, uint32_t height) {
     const size_t t8 = (size_t)((width + 7) / 8) * (size_t)((height + 7) / 8);
     const size_t ta = (size_t)((width + 7) / 8) * (size_t)((height + 15) / 16);
     const size_t tb = (size_t)((width + 15) / 16) * (size_t)((height + 7) / 8);
-    return (size_t)kSchedHeader + 2 * t8 + (ta > tb ? ta : tb) * kFrontierWords;
+    // and the coarse frontiers of their super-tiles (kSuperTiles x kSuperTiles tiles)
+    const size_t k = kSuperTiles;
+    const size_t sa = (((width + 7) / 8 + k - 1) / k) * (((height + 15) / 16 + k - 1) / k);
+    const size_t sb = (((width + 15) / 16 + k - 1) / k) * (((height + 7) / 8 + k - 1) / k);
+    return (size_t)kSchedHeader + 2 * t8 + (ta > tb ? ta : tb) * kFrontierWords + (sa > sb ? sa : sb) * kSuperWords;
 }
 
 cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int nviews,

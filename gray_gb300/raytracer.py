@@ -170,7 +170,7 @@ class Raytracer(torch.nn.Module):
     @torch.no_grad()
     def update_pruning_stats(self):
         g = self.cuda_module.get_gaussians()
-        g.pruning_counter.add_(g.was_visible.to(torch.int32))
+        g.pruning_counter.add_(g.was_visible)  # one kernel: the bool flags are promoted in place
 
     @staticmethod
     def from_safetensors(cfg: RaytracerConfig, path: str, image_width: int, image_height: int,

@@ -128,7 +128,8 @@ typedef struct gray_hitlist {
     uint32_t *pool;           /* [size] */
     uint32_t size;
     uint32_t *schedule;       /* [gray_schedule_words(W_alloc, H_alloc)] work order of the forward's
-                                 pixel tiles (dense tiles first) and each tile's BVH frontier;
+                                 pixel tiles (dense tiles first), each tile's BVH frontier and the
+                                 coarse frontiers of 4x4-tile super-tiles that seed the tiles' walks;
                                  NULL: tiles in launch order, traversals from the root */
 } gray_hitlist;
 
