@@ -212,25 +212,20 @@ def test_forward_captured_in_a_cuda_graph_matches_eager(oracle):
     assert all(np.array_equal(a, b) for a, b in zip(G.hit_lists(rt), eager_lists))
 
 
-@pytest.mark.parametrize("room", ["full", "no_super", "estimates_only", "none"])
-def test_schedule_buffer_sizes_give_the_same_forward(oracle, room):
-    """The forward uses what the caller's schedule buffer holds: the full buffer (tile estimates and
-    order, per-tile frontiers, super-tile frontiers that seed the tile walks), one without room for
-    the super-tiles (tiles walk from the root), one with estimates and order only (packets traverse
-    from the root), or none (tiles in launch order).  The image, transmittances and hit lists are
-    the same in every case and match the oracle."""
+@pytest.mark.parametrize("schedule", [True, False])
+def test_forward_with_and_without_a_schedule_buffer(oracle, schedule):
+    """With the schedule buffer (gray_schedule_words(W, H) words: tile estimates and order, per-tile
+    frontiers, super-tile frontiers seeding the tile walks) the densest tiles run first and packets
+    start at their tile's frontier; without it (NULL) the tiles run in launch order from the root.
+    The image, transmittances and hit lists are the same and match the oracle."""
     sc = synthetic.clustered_scene(40_000, seed=6)
     W, H = 200, 120
     cam = synthetic.orbit_camera(1.1, W, H)
     rt = G.make_tracer(W, H, sc.mean, sc.rotation, sc.scale, sc.opacity,
                        channels=np.full((sc.n, 3), 0.5, np.float32))
-    full = rt.schedule.numel()
-    t8 = ((W + 7) // 8) * ((H + 7) // 8)
-    tiles = max(((W + 7) // 8) * ((H + 15) // 16), ((W + 15) // 16) * ((H + 7) // 8))
-    words = {"full": full, "no_super": 64 + 2 * t8 + tiles * 161, "estimates_only": 64 + 2 * t8, "none": 0}[room]
-    assert words <= full
-    rt.schedule = torch.zeros(words, device="cuda", dtype=torch.int32) if words else None
-    rt._invalidate()
+    if not schedule:
+        rt.schedule = None
+        rt._invalidate()
     ro, rd = _camera_rays_gpu(rt, cam)
     rt.check_status()
     geom, l2w, aabb, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, sc.scale, sc.opacity)
