@@ -1025,6 +1025,66 @@ struct SuperScratch {
     uint32_t leaves[kFrontierSort];
 };
 
+// Bitonic sort of the warp's nf (key, link) frontier entries (fs.key / fs.val, nf <= 32 * E) by key,
+// written to out[1 .. nf].  The network runs in registers: element i sits in lane i % 32, slot i / 32;
+// the partner at distance j < 32 is the same slot of lane ^ j (a shuffle), at j >= 32 the slot
+// e ^ (j / 32) of the same lane.  Padding keys are +inf (sorted last); each pair (lower, upper)
+// swaps iff (ascending ? k_upper < k_lower : k_lower < k_upper), so NaN keys never move and ties
+// keep their places.
+template <int E>
+__device__ __forceinline__ void frontier_sort_out(const FrontierScratch &fs, int nf, uint32_t *out) {
+    const int lane = threadIdx.x & 31;
+    float k[E];
+    uint32_t v[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const int i = e * 32 + lane;
+        k[e] = i < nf ? fs.key[i] : __int_as_float(0x7f800000);
+        v[e] = i < nf ? fs.val[i] : GRAY_NULL;
+    }
+#pragma unroll
+    for (int kk = 2; kk <= 32 * E; kk <<= 1) {
+#pragma unroll
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+#pragma unroll
+                for (int e = 0; e < E; e++) {
+                    const int f = e ^ (j >> 5);
+                    if (f > e) {
+                        const bool up = ((e * 32 + lane) & kk) == 0;
+                        const float kl = k[e], ku = k[f];
+                        if (up ? (ku < kl) : (kl < ku)) {
+                            k[e] = ku;
+                            k[f] = kl;
+                            const uint32_t t = v[e];
+                            v[e] = v[f];
+                            v[f] = t;
+                        }
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < E; e++) {
+                    const float ko = __shfl_xor_sync(kFull, k[e], j);
+                    const uint32_t vo = __shfl_xor_sync(kFull, v[e], j);
+                    const bool up = ((e * 32 + lane) & kk) == 0;
+                    const bool lower = (lane & j) == 0;
+                    const float kl = lower ? k[e] : ko, ku = lower ? ko : k[e];
+                    if (up ? (ku < kl) : (kl < ku)) {
+                        k[e] = ko;
+                        v[e] = vo;
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const int i = e * 32 + lane;
+        if (i < nf) out[1 + i] = v[e];
+    }
+}
+
 // One warp walks the top of the BVH for a pixel rectangle whose frustum is in fs.fr: returns (on
 // every lane) the number of leaves under the frontier, the nodes of at most `cut` leaves (and the
 // leaves) it reaches; with `out`, writes the frontier there sorted front to back (count + entries),
@@ -1226,34 +1286,10 @@ __device__ __forceinline__ uint32_t frontier_walk(const float4 *nodes, int n, ui
         return est;
     }
     if (complete && nf <= kFrontierMax) {
-        // bitonic sort of the entries by key (padding sorts last); NaN keys compare false
-        int p2 = 32;
-        while (p2 < nf) p2 <<= 1;
-        for (int i = nf + lane; i < p2; i += 32) {
-            fs.key[i] = __int_as_float(0x7f800000);
-            fs.val[i] = GRAY_NULL;
-        }
-        __syncwarp();
-        for (int k = 2; k <= p2; k <<= 1) {
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int i = lane; i < p2; i += 32) {
-                    const int ixj = i ^ j;
-                    if (ixj > i) {
-                        const float ki = fs.key[i], kj = fs.key[ixj];
-                        const bool up = (i & k) == 0;
-                        if (up ? (kj < ki) : (ki < kj)) {
-                            fs.key[i] = kj;
-                            fs.key[ixj] = ki;
-                            const uint32_t v = fs.val[i];
-                            fs.val[i] = fs.val[ixj];
-                            fs.val[ixj] = v;
-                        }
-                    }
-                }
-                __syncwarp();
-            }
-        }
-        for (int i = lane; i < nf; i += 32) out[1 + i] = fs.val[i];
+        if (nf <= 32) frontier_sort_out<1>(fs, nf, out);
+        else if (nf <= 64) frontier_sort_out<2>(fs, nf, out);
+        else if (nf <= 128) frontier_sort_out<4>(fs, nf, out);
+        else frontier_sort_out<8>(fs, nf, out);
         if (lane == 0) out[0] = (uint32_t)nf;
     } else if (lane == 0) {
         out[0] = kFrontierNone;
