@@ -404,7 +404,6 @@ def gpu_arm(a, rank, world, local_rank):
         "fold_sh_backward": 64.0 * n + (64.0 + 120.0 + 1.0 + 12.0 + 180.0 + 12.0 + 12.0 + 180.0) * V,
         "adam": (59 * 32.0 + 12.0) * n,  # 59 Adam floats x (p, m, v, g) read + written; channel grads zeroed
         "snapshot": (44.0 + 48 + 48 + 32) * n,
-        "bwd_record": (96.0 + 96.0) * n,
         "refit": 44.0 * n + 24.0 * (2 * n - 1),
     }
     total_ms = sum(v[0] for v in res.values())
@@ -412,9 +411,8 @@ def gpu_arm(a, rank, world, local_rank):
     dom_ms = res[dominant][0] / res[dominant][1]
     peak, peak_kind = measured_peak_gbs()
     achieved = algo.get(dominant, 0.0) / (dom_ms / 1000.0) / 1e9
-    # kernels behind one profiled scope: adam = step count + update; bwd_record = the per-Gaussian
-    # backward record (written by the forward, beside the tile schedule); trace_backward = the replay;
-    # tile_schedule = tile work estimate + bucket scan + scatter (on the library's
+    # kernels behind one profiled scope: adam = step count + update; trace_backward = backward
+    # record + replay; tile_schedule = tile work estimate + bucket scan + scatter (on the library's
     # side stream, beside forward_prep), then trace_forward = the trace (all four in trace_forward
     # when no side stream could be had); refit = block-local climb + upper tree.  The snapshot, the
     # forward preparation and the backward record run a bulk-copy kernel over whole tiles (128, 64
@@ -422,7 +420,7 @@ def gpu_arm(a, rank, world, local_rank):
     def tiled(tile):
         return int(n >= tile) + int(n % tile != 0)
 
-    kernels_per_group = {"adam": 2, "trace_backward": 1, "bwd_record": tiled(128), "refit": 2, "tile_schedule": 3,
+    kernels_per_group = {"adam": 2, "trace_backward": 1 + tiled(128), "refit": 2, "tile_schedule": 3,
                          "trace_forward": 1 if "tile_schedule" in res else 4, "snapshot": tiled(128),
                          "forward_prep": tiled(64)}
     launches = sum(cnt * kernels_per_group.get(name, 1) for name, (_, cnt) in res.items())

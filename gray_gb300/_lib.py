@@ -75,8 +75,8 @@ class ParamsC(ctypes.Structure):
                 ("status", P), ("trace_variant", ctypes.c_int32)]
 
 
-ENTRY_POINTS = ("gray_forward_pass", "gray_forward_pass_display", "gray_backward_pass", "gray_backward_record",
-                "gray_step", "gray_update_bvh", "gray_rebuild_bvh", "gray_sort_tmp_words", "gray_profiler_enable",
+ENTRY_POINTS = ("gray_forward_pass", "gray_forward_pass_display", "gray_backward_pass", "gray_step",
+                "gray_update_bvh", "gray_rebuild_bvh", "gray_sort_tmp_words", "gray_profiler_enable",
                 "gray_profiler_collect", "gray_last_error", "gray_version")
 
 _lib = None
@@ -95,8 +95,8 @@ def load(path: str | None = None):
     if not os.path.exists(path):
         raise GrayError(f"libgray_gb300.so not found at {path}; run `python -m gray_gb300.build`")
     L = ctypes.CDLL(path)
-    for name in ("gray_forward_pass", "gray_forward_pass_display", "gray_backward_pass", "gray_backward_record",
-                 "gray_step", "gray_update_bvh", "gray_rebuild_bvh"):
+    for name in ("gray_forward_pass", "gray_forward_pass_display", "gray_backward_pass", "gray_step",
+                 "gray_update_bvh", "gray_rebuild_bvh"):
         f = getattr(L, name)
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.POINTER(ParamsC), ctypes.c_void_p]

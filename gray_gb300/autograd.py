@@ -145,7 +145,6 @@ class _TraceState:
                 hl.pool[: sv["pool"].numel()].copy_(sv["pool"])
                 t.get_gaussians().channels.copy_(sv["channels"])
                 t.get_gaussians().was_visible.zero_()
-            t.backward_record()  # the record the backward replays with follows the restored colours
             t.generation += 1
         else:
             _set_camera(t, self.camera)

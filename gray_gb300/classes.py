@@ -395,11 +395,6 @@ class Raytracer:
     def backward_pass(self):
         self._call("gray_backward_pass")
 
-    def backward_record(self):
-        """Rewrite the per-Gaussian backward record from the current state (forward_pass does this
-        itself; call it after putting a saved forward's colours and hit lists back by hand)."""
-        self._call("gray_backward_record")
-
     def step(self):
         self._call("gray_step")
 

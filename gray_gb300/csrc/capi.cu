@@ -141,10 +141,6 @@ int forward(const gray_params *p, bool display, cudaStream_t s) {
         if ((e = cudaEventRecord(side.join, side.s)) != cudaSuccess) return cuda_fail(e, "join");
     }
     GRAY_LAUNCH("forward_prep", gray::launch_forward_prep(*p, !display, s));
-    // the backward record from this forward's state (live values and colours just written), on s
-    // while the schedule still runs on the side stream; skipped on the device unless gradients are on
-    if (!display && p->scene.bwd_rec)
-        GRAY_LAUNCH("bwd_record", gray::launch_bwd_record(*p, p->metadata.grads_enabled, s));
     if (overlap) {
         cudaError_t e = cudaStreamWaitEvent(s, side.join, 0);
         if (e != cudaSuccess) return cuda_fail(e, "join");
@@ -231,16 +227,6 @@ int gray_backward_pass(const gray_params *p, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     GRAY_LAUNCH("trace_backward", gray::launch_trace_backward(*p, s));
     GRAY_LAUNCH("fold_sh_backward", gray::launch_fold_and_sh_backward(*p, s));
-    return GRAY_OK;
-}
-
-int gray_backward_record(const gray_params *p, void *stream) {
-    int e = check_trace(p);
-    if (e) return e;
-    if (p->gaussians.sh_is_fp16) return fail(GRAY_ERR_INVALID_ARGUMENT, "backward_record needs an inference_only=False raytracer");
-    if (!p->scene.bwd_rec) return fail(GRAY_ERR_INVALID_ARGUMENT, "missing scene.bwd_rec");
-    cudaStream_t s = (cudaStream_t)stream;
-    GRAY_LAUNCH("bwd_record", gray::launch_bwd_record(*p, nullptr, s));
     return GRAY_OK;
 }
 

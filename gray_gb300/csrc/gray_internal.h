@@ -46,10 +46,6 @@ cudaError_t launch_trace_forward(const gray_params &p, bool display, bool schedu
 size_t gray_schedule_words_for(uint32_t width, uint32_t height);
 // ellipsoid view; a no-op launch unless config.render_ellipsoids is set
 cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s);
-// the per-Gaussian backward record (scene.bwd_rec) from the forward's state; only_if (device flag,
-// may be null): write it only when the flag is set (the forward passes grads_enabled)
-cudaError_t launch_bwd_record(const gray_params &p, const uint8_t *only_if, cudaStream_t s);
-// the reverse replay of the hit lists with the record
 cudaError_t launch_trace_backward(const gray_params &p, cudaStream_t s);
 cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int nviews,
                                uint32_t total_packets, float *out, uint32_t *counter, uint32_t *frontier,

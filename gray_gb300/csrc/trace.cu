@@ -1960,9 +1960,9 @@ __global__ void __launch_bounds__(256) bwd_record_kernel(int first, int n, const
                                                          const float *__restrict__ channels,
                                                          const float4 *__restrict__ l2w,
                                                          const float *__restrict__ eps_scale_grad,
-                                                         float4 *__restrict__ rec, const uint8_t *__restrict__ only_if) {
+                                                         float4 *__restrict__ rec) {
     const int i = first + blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || (only_if && !*only_if)) return;
+    if (i >= n) return;
     const float ls[3] = {scale[3 * i], scale[3 * i + 1], scale[3 * i + 2]};
     const float ch[3] = {channels[3 * i], channels[3 * i + 1], channels[3 * i + 2]};
     float4 r[kRecVec];
@@ -2005,11 +2005,10 @@ __device__ __forceinline__ void rec_issue_loads(RecIn &in, uint64_t *bar, int ti
 __global__ void __launch_bounds__(kRecTile) bwd_record_bulk_kernel(
     int tiles, const float2 *__restrict__ live, const float *__restrict__ scale, const float4 *__restrict__ rotation,
     const float *__restrict__ channels, const float4 *__restrict__ l2w, const float *__restrict__ eps_scale_grad,
-    float4 *__restrict__ rec, int32_t *__restrict__ status, const uint8_t *__restrict__ only_if) {
+    float4 *__restrict__ rec, int32_t *__restrict__ status) {
     __shared__ __align__(16) RecIn in[2];
     __shared__ __align__(16) float4 out[kRecVec * kRecTile];
     __shared__ __align__(8) uint64_t bar[2];
-    if (only_if && !*only_if) return;  // the whole grid reads the same flag
     const int t = threadIdx.x;
     if (t == 0) {
         mbar_init(&bar[0], 1);
@@ -2232,39 +2231,36 @@ __global__ void __launch_bounds__(128) trace_backward_kernel(const BwdArgs a) {
     } while (next_gid(a, cur, gid));
 }
 
-cudaError_t launch_bwd_record(const gray_params &p, const uint8_t *only_if, cudaStream_t s) {
-    const int n = p.gaussians.count;
-    if (n <= 0 || !p.scene.bwd_rec) return cudaSuccess;
-    const float2 *live = reinterpret_cast<const float2 *>(p.scene.live);
-    const float4 *rot = reinterpret_cast<const float4 *>(p.gaussians.rotation);
-    const float4 *l2w = reinterpret_cast<const float4 *>(p.scene.l2w);
-    float4 *rec = reinterpret_cast<float4 *>(p.scene.bwd_rec);
-    const bool bulk = p.status && aligned16(live) && aligned16(p.gaussians.scale) && aligned16(rot) &&
-                      aligned16(p.gaussians.channels) && aligned16(l2w) && aligned16(rec);
-    const int tiles = bulk ? n / kRecTile : 0;
-    cudaError_t e;
-    if (tiles > 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bwd_record_bulk_kernel, kRecTile, 0)) !=
-            cudaSuccess)
-            return e;
-        const int want = sms * (per_sm > 0 ? per_sm : 1);
-        bwd_record_bulk_kernel<<<tiles < want ? tiles : want, kRecTile, 0, s>>>(
-            tiles, live, p.gaussians.scale, rot, p.gaussians.channels, l2w, p.config.eps_scale_grad, rec, p.status,
-            only_if);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    }
-    const int first = tiles * kRecTile;
-    if (first < n)
-        bwd_record_kernel<<<(unsigned int)((n - first + 255) / 256), 256, 0, s>>>(
-            first, n, live, p.gaussians.scale, rot, p.gaussians.channels, l2w, p.config.eps_scale_grad, rec, only_if);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_trace_backward(const gray_params &p, cudaStream_t s) {
     const int n = p.gaussians.count;
+    if (n > 0) {
+        const float2 *live = reinterpret_cast<const float2 *>(p.scene.live);
+        const float4 *rot = reinterpret_cast<const float4 *>(p.gaussians.rotation);
+        const float4 *l2w = reinterpret_cast<const float4 *>(p.scene.l2w);
+        float4 *rec = reinterpret_cast<float4 *>(p.scene.bwd_rec);
+        const bool bulk = p.status && aligned16(live) && aligned16(p.gaussians.scale) && aligned16(rot) &&
+                          aligned16(p.gaussians.channels) && aligned16(l2w) && aligned16(rec);
+        const int tiles = bulk ? n / kRecTile : 0;
+        cudaError_t e;
+        if (tiles > 0) {
+            int dev = 0, sms = 0, per_sm = 0;
+            if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+            if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bwd_record_bulk_kernel, kRecTile, 0)) !=
+                cudaSuccess)
+                return e;
+            const int want = sms * (per_sm > 0 ? per_sm : 1);
+            bwd_record_bulk_kernel<<<tiles < want ? tiles : want, kRecTile, 0, s>>>(
+                tiles, live, p.gaussians.scale, rot, p.gaussians.channels, l2w, p.config.eps_scale_grad, rec,
+                p.status);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
+        const int first = tiles * kRecTile;
+        if (first < n)
+            bwd_record_kernel<<<(unsigned int)((n - first + 255) / 256), 256, 0, s>>>(
+                first, n, live, p.gaussians.scale, rot, p.gaussians.channels, l2w, p.config.eps_scale_grad, rec);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     BwdArgs a;
     a.alloc_w = p.image_width;
     a.render_w = p.render_width;

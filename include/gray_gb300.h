@@ -240,25 +240,15 @@ size_t gray_schedule_words(uint32_t width, uint32_t height);
 
 /* Raytracer::forward_pass (cuda/raytracer.h:88-102): counts the call, resets the backward
  * hit list and was_visible, evaluates SH colours (if enable_sh) and traces the render
- * rectangle.  grads_enabled must have been set by the caller (MetaDataHolder::update).  With
- * gradients enabled on a training tracer (scene.bwd_rec given) it also writes the per-Gaussian
- * backward record that gray_backward_pass replays with (from this forward's live values and
- * colours). */
+ * rectangle.  grads_enabled must have been set by the caller (MetaDataHolder::update). */
 int gray_forward_pass(const gray_params *p, void *stream);
 
 /* Raytracer::forward_pass_display (cuda/raytracer.h:104-114): SH + trace, no resets. */
 int gray_forward_pass_display(const gray_params *p, void *stream);
 
 /* Raytracer::backward_pass (cuda/raytracer.h:116-124): reverse replay of the hit lists into the
- * gradient arrays (and pruning_weight, was_visible), then the SH backward.  It uses the backward
- * record the last gradient-enabled gray_forward_pass wrote. */
+ * gradient arrays (and pruning_weight, was_visible), then the SH backward. */
 int gray_backward_pass(const gray_params *p, void *stream);
-
-/* Rewrites the per-Gaussian backward record (scene.bwd_rec) from the current live values, colours,
- * parameters and snapshot.  No reference counterpart: gray_forward_pass does this itself; a caller
- * that puts a saved forward's state back by hand (colours, hit lists, per-pixel state) calls it
- * before gray_backward_pass. */
-int gray_backward_record(const gray_params *p, void *stream);
 
 /* Raytracer::step (cuda/raytracer.h:126-133 -> cuda/opt/adam.cu:70-83): total_num_steps += 1
  * and one fused Adam step over all parameter groups (SH every sh_update_laziness steps). */

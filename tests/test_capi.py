@@ -127,14 +127,3 @@ def test_copy_wait_selftest_checks_its_arguments(gray_lib):
     assert L.gray_selftest_copy_wait(None, 1000, None) == 1  # GRAY_ERR_INVALID_ARGUMENT
     assert b"status" in L.gray_last_error()
     assert L.gray_selftest_copy_wait(ctypes.c_void_p(16), 3_000_000_000, None) == 3  # GRAY_ERR_OUT_OF_RANGE
-
-
-def test_backward_record_checks_its_arguments(gray_lib):
-    """gray_backward_record refuses a missing record buffer before any launch (a tracer without one
-    has no backward)."""
-    from gray_gb300 import _lib
-
-    p = _lib.ParamsC()
-    p.image_width = p.image_height = p.render_width = p.render_height = 16
-    with pytest.raises(_lib.GrayError):
-        _lib.call("gray_backward_record", p, 0)
