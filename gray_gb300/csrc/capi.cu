@@ -32,8 +32,8 @@ int check_common_impl(const gray_params *p) {
         return fail(GRAY_ERR_OUT_OF_RANGE, "render resolution must be positive and within the allocated framebuffer");
     if ((size_t)p->image_width * (size_t)p->image_height >= (size_t)0xFFFFFFFFu)
         return fail(GRAY_ERR_OUT_OF_RANGE, "framebuffer too large for 32-bit pixel ids");
-    if (p->gaussians.count > 0x7FFFFFFF - 1 || (uint32_t)p->gaussians.count >= 0x80000000u)
-        return fail(GRAY_ERR_OUT_OF_RANGE, "too many Gaussians");
+    if (p->gaussians.count > (1 << 30))  // the BVH's parent words keep bit 30 for a flag
+        return fail(GRAY_ERR_OUT_OF_RANGE, "too many Gaussians (at most 2^30)");
     return GRAY_OK;
 }
 

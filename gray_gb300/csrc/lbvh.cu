@@ -10,8 +10,10 @@
 //
 // Node layout (16 floats): child0 box (minx miny minz maxx maxy maxz), child1 box, child0 link,
 // child1 link, leaves below the node, leaves below child0 (both as uint32 bits).  A link with
-// GRAY_LEAF_BIT set names a Gaussian; otherwise an internal node.  Everything here is
-// deterministic; the CPU oracle restates it bit-exactly.
+// GRAY_LEAF_BIT set names a Gaussian; otherwise an internal node.  Parents (int_parent per internal
+// node, leaf_parent per sorted leaf) carry kSecondChild when the node or leaf is its parent's second
+// child, so a refit knows which child box it fills without reading the parent; the root's parent
+// is -1.  Everything here is deterministic; the CPU oracle restates it bit-exactly.
 #include "gray_device.cuh"
 #include "gray_internal.h"
 
@@ -249,6 +251,9 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(int n, int 
 // ---------------------------------------------------------------------------------------------
 // Karras (2012) hierarchy over sorted codes; ties broken by sorted position.
 // ---------------------------------------------------------------------------------------------
+constexpr int32_t kSecondChild = 1 << 30;  // parent-word flag: the second child (counts are below 2^30)
+constexpr int32_t kParentMask = kSecondChild - 1;
+
 __device__ __forceinline__ int lbvh_delta(const uint32_t *codes, int n, int i, int j) {
     if (j < 0 || j > n - 1) return -1;
     uint32_t a = codes[i], b = codes[j];
@@ -287,10 +292,10 @@ __global__ void karras_kernel(int n, const uint32_t *__restrict__ codes, const u
     }
     if (hi_i == gamma + 1) {
         c1 = order[gamma + 1] | GRAY_LEAF_BIT;
-        leaf_parent[gamma + 1] = i;
+        leaf_parent[gamma + 1] = i | kSecondChild;
     } else {
         c1 = (uint32_t)(gamma + 1);
-        int_parent[gamma + 1] = i;
+        int_parent[gamma + 1] = i | kSecondChild;
     }
     // words 14 and 15: leaves below the node and below its first child (the forward's frontier
     // walk reads them)
@@ -334,8 +339,8 @@ __global__ void refit_kernel(int n, const float4 *__restrict__ aabb, const uint3
     uint32_t gid = order[k];
     float4 a = aabb[2 * gid], b = aabb[2 * gid + 1];
     float box[6] = {a.x, a.y, a.z, b.x, b.y, b.z};
-    int p = n > 1 ? leaf_parent[k] : -1;
-    if (p < 0) {
+    int pw = n > 1 ? leaf_parent[k] : -1;  // parent word: index | kSecondChild, or -1
+    if (pw < 0) {
         root_box[0] = box[0];
         root_box[1] = box[1];
         root_box[2] = box[2];
@@ -346,10 +351,9 @@ __global__ void refit_kernel(int n, const float4 *__restrict__ aabb, const uint3
         root_box[7] = 0.0f;
         return;
     }
-    uint32_t link = gid | GRAY_LEAF_BIT;
     for (int guard = 0; guard < 128; guard++) {
-        uint32_t c0 = __float_as_uint(__ldcg(nodes + 16 * (size_t)p + 12));
-        store_child_box(nodes, p, c0 == link ? 0 : 1, box);
+        const int p = pw & kParentMask;
+        store_child_box(nodes, p, (pw & kSecondChild) ? 1 : 0, box);
         if (add_acq_rel(&flags[p], 1u) == 0u) return;
         const float *nd = nodes + 16 * (size_t)p;
         float u[6];
@@ -360,8 +364,8 @@ __global__ void refit_kernel(int n, const float4 *__restrict__ aabb, const uint3
         }
 #pragma unroll
         for (int q = 0; q < 6; q++) box[q] = u[q];
-        int pp = int_parent[p];
-        if (pp < 0) {
+        pw = int_parent[p];
+        if (pw < 0) {
             root_box[0] = box[0];
             root_box[1] = box[1];
             root_box[2] = box[2];
@@ -372,8 +376,6 @@ __global__ void refit_kernel(int n, const float4 *__restrict__ aabb, const uint3
             root_box[7] = 0.0f;
             return;
         }
-        link = (uint32_t)p;
-        p = pp;
     }
     refit_gave_up(status);
 }
@@ -429,14 +431,15 @@ __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const floa
     const uint32_t gid = order[k];
     const float4 a = aabb[2 * gid], b = aabb[2 * gid + 1];
     float box[6] = {a.x, a.y, a.z, b.x, b.y, b.z};
-    int p = n > 1 ? leaf_parent[k] : -1;
-    if (p < 0) {
+    int pw = n > 1 ? leaf_parent[k] : -1;  // parent word: index | kSecondChild, or -1
+    if (pw < 0) {
         write_root_box(root_box, box);
         return;
     }
     int lo = k, hi = k;
-    uint32_t link = gid | GRAY_LEAF_BIT;
     for (int guard = 0; guard < 128; guard++) {
+        const int p = pw & kParentMask;
+        const int slot = (pw & kSecondChild) ? 1 : 0;
         const bool in_block = p >= base && p < base + kThreads;
         uint4 q3;
         int pnext;
@@ -447,7 +450,6 @@ __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const floa
             q3 = __ldcg(reinterpret_cast<const uint4 *>(nodes) + 4 * (size_t)p + 3);
             pnext = int_parent[p];
         }
-        const int slot = q3.x == link ? 0 : 1;
         const int leaves = (int)q3.z;
         const int plo = slot == 0 ? lo : hi - leaves + 1, phi = slot == 0 ? lo + leaves - 1 : hi;
         if (plo < base || phi >= base + kThreads) {
@@ -482,9 +484,8 @@ __global__ void __launch_bounds__(kThreads) refit_local_kernel(int n, const floa
         }
         lo = plo;
         hi = phi;
-        link = (uint32_t)p;
-        p = pnext;
-        if (p < 0) {
+        pw = pnext;
+        if (pw < 0) {
             write_root_box(root_box, box);
             return;
         }
@@ -500,21 +501,22 @@ __global__ void __launch_bounds__(kThreads) refit_top_kernel(const int32_t *__re
     if (i >= queue[0]) return;
     int p = (int)queue[1 + i];
     for (int guard = 0; guard < 128; guard++) {
-        // both child boxes of p are complete
+        // both child boxes of p are complete; its parent word (index and which child p is) is read
+        // with them, so a level costs one load round trip and one atomic
         const float *nd = nodes + 16 * (size_t)p;
+        const int pw = int_parent[p];
         float box[6];
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             box[q] = fminf(__ldcg(nd + q), __ldcg(nd + 6 + q));
             box[3 + q] = fmaxf(__ldcg(nd + 3 + q), __ldcg(nd + 9 + q));
         }
-        const int pp = int_parent[p];
-        if (pp < 0) {
+        if (pw < 0) {
             write_root_box(root_box, box);
             return;
         }
-        const uint32_t c0 = __float_as_uint(__ldcg(nodes + 16 * (size_t)pp + 12));
-        store_child_box(nodes, pp, c0 == (uint32_t)p ? 0 : 1, box);
+        const int pp = pw & kParentMask;
+        store_child_box(nodes, pp, (pw & kSecondChild) ? 1 : 0, box);
         if (add_acq_rel(&flags[pp], 1u) == 0u) return;
         p = pp;
     }

@@ -142,8 +142,9 @@ typedef struct gray_scene {
     float *live;        /* [N,2]  per-forward (sigmoid(opacity), scaling factor)      */
     float *grad_acc;    /* [N,16] backward accumulators, zero between passes          */
     float *nodes;       /* [max(N-1,1),16] BVH2 nodes: child boxes + child links      */
-    int32_t *int_parent;  /* [max(N-1,1)] */
-    int32_t *leaf_parent; /* [N] indexed by sorted leaf position */
+    int32_t *int_parent;  /* [max(N-1,1)] parent of each internal node, with bit 30 set when the
+                             node is its parent's second child; -1 for the root */
+    int32_t *leaf_parent; /* [N] indexed by sorted leaf position, same encoding */
     uint32_t *order;      /* [N] sorted leaf position -> gaussian id */
     uint32_t *codes;      /* [N] Morton codes in sorted order */
     uint32_t *refit_flags;/* [max(N-1,1)] */
