@@ -13,7 +13,8 @@ state) are far larger than L2, so no flush is needed between steps.
 Prints one JSON line (rank 0).  `value` is train-steps/s with the target image resident in HBM;
 `e2e` is the same step through the public Raytracer API with the target copied from pinned host
 memory and the loss read back every step (the upload of step i+1 runs on a copy stream during step
-i; `e2e.serial_value` is the same with upload and step in series).  `roofline` is for the kernel with the largest share of
+i; `e2e.serial_value` is the same with upload and step in series; each of the three timed loops starts
+from the same training state, since training moves the Gaussians and their cost).  `roofline` is for the kernel with the largest share of
 the step, from CUDA events recorded around each launch inside the timed region.  `--impl
 reference` times the CPU restatement of the reference's algorithm (oracle/, the reference itself
 needs OptiX and does not build here) on a bounded sample of rays per step, extrapolated.
@@ -358,6 +359,25 @@ def gpu_arm(a, rank, world, local_rank):
     torch.cuda.synchronize()
     rt.cuda_module.check_status()
 
+    # Every train step moves the Gaussians (Adam on a random target), and their cost per step moves
+    # with them (about 7% over 150 steps of this workload).  Each timed segment below therefore starts
+    # from the same training state, restored before it: parameters, gradients, Adam moments, pruning
+    # statistics, SH degree, step counter, and the snapshot + refit that follow from them.
+    state_names = [k + n for k in ("", "grad_", "first_moment_", "second_moment_")
+                   for n in ("mean", "rotation", "scale", "opacity", "channels", "sh_coeffs_dc", "sh_coeffs_rest")]
+    state_names += ["pruning_weight", "pruning_counter", "was_visible", "marked", "current_sh_degree"]
+    gh, meta = rt.cuda_module.get_gaussians(), rt.cuda_module.get_metadata()
+    start_state = {n: getattr(gh, n).clone() for n in state_names}
+    start_steps = meta.total_num_steps.clone()
+
+    def restore_start_state():
+        with torch.no_grad():
+            for n, t in start_state.items():
+                getattr(gh, n).copy_(t)
+            meta.total_num_steps.copy_(start_steps)
+        rt.cuda_module.update_bvh()
+        torch.cuda.synchronize()
+
     # ---- timed region: device-resident inputs ----
     st = rt.cuda_module.get_stats()
     st.reset()
@@ -376,11 +396,13 @@ def gpu_arm(a, rank, world, local_rank):
     ms_step = ms / a.steps
     steps_per_s = whole_job_rate(a.steps, ms, world)
 
-    # ---- e2e through the public API with host buffers ----
+    # ---- e2e through the public API with host buffers (from the same training state) ----
     for _ in range(max(1, a.warmup // 2)):
         e2e_step()
-    ms_e2e_serial = timed(e2e_step, a.steps)
     e2e_run(2)
+    restore_start_state()
+    ms_e2e_serial = timed(e2e_step, a.steps)
+    restore_start_state()
     ms_e2e = timed(lambda: e2e_run(a.steps), 1)
     e2e_steps_per_s = whole_job_rate(a.steps, ms_e2e, world)
 
