@@ -235,6 +235,49 @@ def test_forward_with_and_without_a_schedule_buffer(oracle, schedule):
     _compare_forward(rt, fwd)
 
 
+def test_forwards_from_two_host_threads_match_their_serial_results():
+    """Each host thread gets its own side stream for the tile schedule (per thread and CUDA context):
+    two threads, each with its own tracer and torch stream, running forwards at the same time give
+    the images and hit lists each tracer gives alone."""
+    import threading
+
+    scenes = [synthetic.clustered_scene(20_000, seed=s) for s in (21, 22)]
+    cams = [synthetic.orbit_camera(0.4 + i, 96, 64) for i in range(2)]
+    rts = [G.make_tracer(96, 64, sc.mean, sc.rotation, sc.scale, sc.opacity,
+                         channels=np.full((sc.n, 3), 0.5, np.float32)) for sc in scenes]
+    alone = []
+    for rt, cam in zip(rts, cams):
+        _camera_rays_gpu(rt, cam)
+        alone.append((G.fb_numpy(rt)["output_channels"], G.hit_lists(rt)))
+    for rt in rts:
+        rt.get_framebuffer().output_channels.zero_()
+    torch.cuda.synchronize()
+    errors = []
+
+    def work(i):
+        try:
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                for _ in range(3):
+                    with torch.enable_grad():
+                        rts[i].forward_pass()
+            s.synchronize()
+        except Exception as e:  # reported below, on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    torch.cuda.synchronize()
+    for rt, (img, lists) in zip(rts, alone):
+        rt.check_status()
+        assert np.array_equal(G.fb_numpy(rt)["output_channels"], img)
+        assert all(np.array_equal(a, b) for a, b in zip(G.hit_lists(rt), lists))
+
+
 def _camera_rays_gpu(rt, cam):
     rt.get_camera().znear.fill_(0.0)
     rt.get_camera().zfar.fill_(99999.9)
