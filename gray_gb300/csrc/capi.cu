@@ -93,19 +93,31 @@ namespace {
 
 // The calling thread's second stream in one CUDA context, with a fork and a join event; made on first
 // use in that context (highest priority: the forward's tile schedule, which it carries, is on the
-// critical path) and kept until the process exits.
+// critical path) and released when the thread exits.
 struct SideStream {
     unsigned long long ctx;
     cudaStream_t s;
     cudaEvent_t fork, join;
 };
-thread_local std::vector<SideStream> t_side;
+struct SideStreams {
+    std::vector<SideStream> v;
+    ~SideStreams() {
+        // work still queued on a stream completes before its resources go; a context already
+        // torn down (process exit, cudaDeviceReset) only makes these calls return an error
+        for (const SideStream &x : v) {
+            cudaEventDestroy(x.fork);
+            cudaEventDestroy(x.join);
+            cudaStreamDestroy(x.s);
+        }
+    }
+};
+thread_local SideStreams t_side;
 
 // false when no side stream can be had (no context id, or a creation failed): run serially
 bool side_stream(SideStream *out) {
     unsigned long long id = 0;
     if (!gray::current_context_id(&id)) return false;
-    for (const SideStream &x : t_side)
+    for (const SideStream &x : t_side.v)
         if (x.ctx == id) {
             *out = x;
             return true;
@@ -122,7 +134,7 @@ bool side_stream(SideStream *out) {
         cudaGetLastError();  // leave no stale error for the launches that follow
         return false;
     }
-    t_side.push_back(x);
+    t_side.v.push_back(x);
     *out = x;
     return true;
 }
