@@ -471,8 +471,7 @@ class Raytracer:
                 n for bit, n in ((1, "backward hit list overflow (increase ppll_backward_size)"),
                                  (2, "BVH traversal limit exceeded"), (4, "refit budget exhausted"),
                                  (8, "render_ellipsoids=True is only supported for no-grad display renders"),
-                                 (16, "a bulk copy did not complete (streaming kernel stopped early)"),
-                                 (32, "a forward warp waited too long for its tile (stopped early)"))
+                                 (16, "a bulk copy did not complete (streaming kernel stopped early)"))
                 if v & bit))
 
     def scene_workspace(self):

@@ -985,90 +985,6 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_claim_kernel(
     }
 }
 
-// Persistent launch with the block's tiles pipelined across its warps: the warps take packets from a
-// block-local sequence (packet k is quarter k % 4 of the block's k / 4-th tile), and the warp that
-// takes a tile's first packet claims the next tile of the schedule's densest-first order for the
-// block.  A warp that finishes its packet goes on to the block's next packet instead of waiting at a
-// block barrier for the tile's slowest one, while a tile's four packets still run on one SM and share
-// its L1.  Frontiers are read from the schedule buffer.  The ids of the block's last kPipeRing tiles
-// are kept in shared memory; a slot is reused once all four packets of its previous tile have read
-// it.  Every wait is bounded (kPipeWaitNs), after which the kernel reports GRAY_STATUS_SCHED_TIMEOUT
-// and the warp stops.
-constexpr int kPipeRing = 8;
-constexpr uint32_t kPipeEnd = 0xFFFFFFFFu;
-constexpr uint64_t kPipeWaitNs = 1000000000ull;
-
-struct PipeRing {
-    uint32_t tile[kPipeRing];  // global tile id, or kPipeEnd once the schedule is exhausted
-    int ready[kPipeRing];      // block-local tile number whose id the slot holds
-    int readers[kPipeRing];    // packets of that tile that have not read the id yet
-    uint32_t next;             // block-local packet sequence
-};
-
-// Lane 0 of the calling warp waits until *v == want or limit_ns have passed; every lane gets whether
-// the value was seen.
-__device__ __forceinline__ bool warp_wait_equal(const int *v, int want, uint64_t limit_ns) {
-    int ok = 1;
-    if ((threadIdx.x & 31) == 0) {
-        uint64_t t0 = 0;
-        while (*reinterpret_cast<const volatile int *>(v) != want) {
-            const uint64_t now = globaltimer_ns();
-            if (t0 == 0) {
-                t0 = now;
-            } else if (now - t0 > limit_ns) {
-                ok = 0;
-                break;
-            }
-        }
-        __threadfence_block();
-    }
-    return __shfl_sync(kFull, ok, 0) != 0;
-}
-
-template <int KB, int MINB>
-__global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_pipe_kernel(const FwdArgs a) {
-    __shared__ FwdShared<KB> sh;
-    __shared__ PipeRing ring;
-    if (*a.render_ellipsoids) return;
-    const int lane = threadIdx.x & 31;
-    if (threadIdx.x < kPipeRing) {
-        ring.ready[threadIdx.x] = (int)threadIdx.x - kPipeRing;  // no tile number matches yet
-        ring.readers[threadIdx.x] = 0;
-    }
-    if (threadIdx.x == 0) ring.next = 0u;
-    __syncthreads();  // the kernel's only block barrier
-    for (;;) {
-        uint32_t k = 0u;
-        if (lane == 0) k = atomicAdd(&ring.next, 1u);
-        k = __shfl_sync(kFull, k, 0);
-        const int T = (int)(k / (uint32_t)kWarps), sub = (int)(k % (uint32_t)kWarps), slot = T % kPipeRing;
-        bool ok = true;
-        if (sub == 0) {
-            // the slot's previous tile (T - kPipeRing) has been read by all its packets
-            ok = warp_wait_equal(&ring.readers[slot], 0, kPipeWaitNs);
-            if (ok && lane == 0) {
-                const uint32_t g = atomicAdd(a.schedule, 1u);
-                ring.tile[slot] = g < (uint32_t)a.ntiles ? a.schedule[kSchedHeader + a.ntiles + g] : kPipeEnd;
-                ring.readers[slot] = kWarps;
-                __threadfence_block();
-                *reinterpret_cast<volatile int *>(&ring.ready[slot]) = T;
-            }
-        }
-        ok = ok && warp_wait_equal(&ring.ready[slot], T, kPipeWaitNs);
-        if (!ok) {
-            if (lane == 0) raise_status(a.status, GRAY_STATUS_SCHED_TIMEOUT);
-            break;
-        }
-        const uint32_t tile = *reinterpret_cast<const volatile uint32_t *>(&ring.tile[slot]);
-        __syncwarp();
-        if (lane == 0) atomicSub(&ring.readers[slot], 1);
-        if (tile == kPipeEnd) break;
-        forward_packet<KB, (MINB < 6)>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x),
-                                       sub % kBlockWarpsX, sub / kBlockWarpsX, a.frontier,
-                                       tile * (uint32_t)kFrontierWords, sh);
-    }
-}
-
 // ---------------------------------------------------------------------------------------------
 // Work order of the forward's tiles and their BVH frontiers.  A tile's work follows the number of
 // Gaussians its rays meet (per-packet time correlates 0.92 with hits), so the estimate is the number
@@ -1831,12 +1747,10 @@ static FwdPlan plan_forward(const gray_params &p, bool display) {
     a = forward_args(p, display);
     // variant: bits 0-1 select (buffer size, register cap), bit 2 the packet shape, bits 3-4 the
     // tile frontier's cut (64 leaves, 32, 128, no frontier), bit 5 packets claimed per warp
-    // (trace_forward_claim_kernel) instead of tiles per block, bit 6 the block's tiles pipelined
-    // across its warps (trace_forward_pipe_kernel)
+    // (trace_forward_claim_kernel) instead of tiles per block
     const int v = p.trace_variant > 0 ? p.trace_variant : kDefaultTraceVariant;
     const int fcut = (v >> 3) & 3;
     const bool claim = (v & 32) != 0;
-    const bool pipe = !claim && (v & 64) != 0;
     a.tile_w = (v & 4) ? 4 : 8;
     a.tile_h = 32 / a.tile_w;
     q.bw = a.tile_w * kBlockWarpsX;
@@ -1850,7 +1764,6 @@ static FwdPlan plan_forward(const gray_params &p, bool display) {
 #define GRAY_FWD_KERNEL(KB, MINB)                                                                   \
     (!q.sched ? reinterpret_cast<const void *>(&trace_forward_kernel<KB, MINB>)                     \
      : claim  ? reinterpret_cast<const void *>(&trace_forward_claim_kernel<KB, MINB>)               \
-     : pipe   ? reinterpret_cast<const void *>(&trace_forward_pipe_kernel<KB, MINB>)                \
               : reinterpret_cast<const void *>(&trace_forward_sched_kernel<KB, MINB>))
     switch (v & 3) {
         case 0: q.kern = GRAY_FWD_KERNEL(32, 1); break;

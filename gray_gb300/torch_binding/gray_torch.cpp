@@ -390,7 +390,6 @@ struct Raytracer : torch::CustomClassHolder {
         if (v & GRAY_STATUS_REFIT_TIMEOUT) return "BVH refit gave up (corrupt tree)";
         if (v & GRAY_STATUS_BAD_MODE) return "render_ellipsoids=True is only supported for no-grad display renders";
         if (v & GRAY_STATUS_COPY_TIMEOUT) return "a bulk copy did not complete (streaming kernel stopped early)";
-        if (v & GRAY_STATUS_SCHED_TIMEOUT) return "a forward warp waited too long for its tile (stopped early)";
         return "unknown device status";
     }
 

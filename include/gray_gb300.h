@@ -47,8 +47,6 @@ extern "C" {
                                              (reference: assertion, gray/raytracer.py:142-144) */
 #define GRAY_STATUS_COPY_TIMEOUT 16       /* a bulk (TMA) copy of a streaming kernel did not complete
                                              within its wait limit; the kernel stopped early */
-#define GRAY_STATUS_SCHED_TIMEOUT 32      /* a warp of the tile-pipelined forward (variant bit 6) waited
-                                             beyond its limit for its tile; the warp stopped early */
 
 /* Gaussian parameters and optimiser state (cuda/core/gaussians.h:7-65). */
 typedef struct gray_gaussians {
