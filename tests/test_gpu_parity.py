@@ -330,6 +330,73 @@ def test_small_scene_sh_camera_and_passes(oracle):
     _grad_close(g.grad_mean.cpu().numpy(), gmean)
 
 
+@pytest.mark.parametrize("exp_power, a_thr, gsf", [(1.0, 0.01, 1.0), (3.0, 0.01, 1.0), (2.5, 0.05, 1.0),
+                                                   (2.0, 0.01, 1.5)])
+def test_response_powers_alpha_threshold_and_scale_factor(oracle, exp_power, a_thr, gsf):
+    """The reference's other Gaussian responses (exp_power 1 and 3 of its high- and low-quality
+    presets, and a general power through pow), a higher alpha threshold and a global scale factor
+    (applied by the snapshot, not by the backward, cuda/backward_pass.cu:101): scaling factor,
+    response, hit lists and images bit-exact against the oracle, and the backward's gradients (whose
+    d|x|^2 term depends on the power) within the gradient bar."""
+    sc = synthetic.small_scene(seed=7, n=200)
+    cam = synthetic.camera_small(96, 96, 96.0)
+    rng = np.random.default_rng(8)
+    chan = rng.uniform(0.0, 1.0, (sc.n, 3)).astype(np.float32)
+    rt = G.make_tracer(96, 96, sc.mean, sc.rotation, sc.scale, sc.opacity, channels=chan, exp_power=exp_power,
+                       alpha_threshold=a_thr)
+    if gsf != 1.0:
+        rt.get_config().global_scale_factor.fill_(gsf)
+        rt.rebuild_bvh()
+    ro, rd = _camera_rays_gpu(rt, cam)
+    geom, l2w, aabb, vis = oracle.snapshot(sc.mean, sc.rotation, sc.scale, np.asarray(sc.opacity).reshape(-1), a_thr,
+                                           exp_power, gsf)
+    live = oracle.forward_prep(np.asarray(sc.opacity).reshape(-1), a_thr, exp_power)
+    ws = rt.scene_workspace()
+    assert np.array_equal(ws.geom.cpu().numpy(), geom)
+    cfg = oracle.TraceConfig(exp_power=exp_power, alpha_threshold=a_thr)
+    fwd = oracle.trace_forward(ro, rd, geom, live, chan, vis, cfg)
+    _compare_forward(rt, fwd)
+    assert fwd["nhit"].sum() > 500
+    gout = rng.standard_normal((96 * 96, 3)).astype(np.float32)
+    rt.get_framebuffer().grad_output_channels.copy_(torch.from_numpy(gout).reshape(96, 96, 3))
+    rt.backward_pass()
+    torch.cuda.synchronize()
+    rt.check_status()
+    ref = oracle.trace_backward(96, 96, ro, rd, fwd, gout, geom, l2w, sc.opacity, sc.scale, sc.rotation, chan, cfg)
+    g = rt.get_gaussians()
+    _grad_close(g.grad_rotation.cpu().numpy(), ref[:, 0:4])
+    _grad_close(g.grad_mean.cpu().numpy(), ref[:, 4:7])
+    _grad_close(g.grad_opacity.cpu().numpy(), ref[:, 7:8])
+    _grad_close(g.grad_scale.cpu().numpy(), ref[:, 8:11])
+    _grad_close(g.grad_channels.cpu().numpy(), ref[:, 12:15])
+
+
+def test_jittered_primary_rays_match_the_oracle_on_the_same_rays(oracle):
+    """jitter_primary_rays: each pixel's ray goes through a hashed sub-pixel offset (changing with the
+    call count), so the packets fall back to per-ray traversal.  The rays the forward wrote differ from
+    the pixel-centre rays by less than a pixel, change from one call to the next, and traced again by
+    the oracle give the same hits, lists and images."""
+    sc = synthetic.small_scene(seed=12, n=150)
+    cam = synthetic.camera_small(64, 64, 64.0)
+    rt = G.make_tracer(64, 64, sc.mean, sc.rotation, sc.scale, sc.opacity, sh_dc=sc.sh_dc, sh_rest=sc.sh_rest,
+                       sh_degree=3)
+    ro0, rd0 = _camera_rays_gpu(rt, cam)  # pixel centres
+    rt.get_config().jitter_primary_rays.fill_(True)
+    rt.get_stats().reset()  # the hit counters accumulate over forwards
+    ro, rd = _camera_rays_gpu(rt, cam)
+    rt.check_status()
+    cos = np.clip((rd * rd0).sum(1) / np.linalg.norm(rd, axis=1) / np.linalg.norm(rd0, axis=1), -1.0, 1.0)
+    pixel_angle = cam.fov_y / 64
+    assert (np.arccos(cos) > 0).mean() > 0.9 and np.arccos(cos).max() < pixel_angle
+    chan = oracle.sh_forward(3, sc.mean, cam.origin.astype(np.float32), sc.sh_dc[:, 0, :], sc.sh_rest)
+    geom, l2w, aabb, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, sc.scale, sc.opacity)
+    fwd = oracle.trace_forward(ro, rd, geom, live, chan, vis, oracle.TraceConfig(t_threshold=0.03))
+    _compare_forward(rt, fwd)
+    assert fwd["nhit"].sum() > 300
+    _, rd2 = _camera_rays_gpu(rt, cam)  # the next call's offsets differ
+    assert not np.array_equal(rd2, rd)
+
+
 def test_multipass_selection_and_segments(oracle):
     """Many faint Gaussians on the same rays with t_threshold = 0: rays composite hundreds of hits,
     crossing many 32-slot passes; the hit list chains one segment per traversal."""
