@@ -67,10 +67,8 @@ def _check(L, rc, what):
 DEFAULT_VARIANT, DEFAULT_BLOCKS_PER_SM = 7, 6
 # candidates the autotuner tries: (kernel variant, persistent blocks per SM), each variant with the
 # block counts around its residency limit (32-entry buffers: 4 per SM; 16 entries uncapped: 3;
-# 16 entries capped: 6), with packets claimed per warp and (variant bit 6) 2x2 packet groups claimed
-# per block
-TUNE_CANDIDATES = [(1, 4), (5, 4), (2, 3), (6, 3), (3, 5), (3, 6), (7, 5), (7, 6),
-                   (64 + 1, 4), (64 + 5, 4), (64 + 3, 6), (64 + 7, 6)]
+# 16 entries capped: 6)
+TUNE_CANDIDATES = [(1, 4), (5, 4), (2, 3), (6, 3), (3, 5), (3, 6), (7, 5), (7, 6)]
 
 
 @dataclass

@@ -1583,77 +1583,23 @@ __global__ void __launch_bounds__(32) batch_frontier_kernel(const gray_batch_sce
     frontier_walk<false>(reinterpret_cast<const float4 *>(bs.nodes), bs.n, cut, fs, nullptr, out, nullptr);
 }
 
-// Per-block shared memory of the batch kernels.
-template <int KB>
-struct BatchShared {
-    unsigned long long kbuf[KB][kFwdThreads];
-    Frustum sfr[kWarps];
-    uint32_t sstk[kWarps][kWideStack];
-    uint32_t scand[kWarps][kQueue];
-    CandCache scc[kWarps];
-    // the packet's scene and view parameters live in shared memory (read where used), which keeps
-    // them out of the registers the traversal needs
-    TraceScene s_sc[kWarps];
-    TraceKnobs s_k[kWarps];
-};
-
-// Packet `local` (row-major over the view's packet grid) of view vw, traced by the calling warp;
-// front_base + front_off: the BVH frontier of its 2x2 packet group (null: from the root).
-template <int KB, bool LO>
-__device__ __forceinline__ void batch_packet(const gray_batch_scene *scenes, const gray_batch_view &vw,
-                                             uint32_t local, int tile_w, float *out, const uint32_t *front_base,
-                                             uint32_t front_off, int32_t *status, BatchShared<KB> &sh) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tile_h = 32 / tile_w;
-    const gray_batch_scene &bs = scenes[vw.scene];
-    const uint32_t tiles_x = (vw.width + tile_w - 1) / tile_w;
-    const int px = (int)((local % tiles_x) * tile_w) + lane % tile_w;
-    const int py = (int)((local / tiles_x) * tile_h) + lane / tile_w;
-    const bool inside = px < (int)vw.width && py < (int)vw.height;
-    if (lane == 0) {
-        TraceKnobs &k = sh.s_k[warp];
-        k.znear = vw.znear;
-        k.zfar = vw.zfar;
-        k.athr = bs.alpha_threshold;
-        k.pw = bs.exp_power;
-        k.tthr = bs.t_threshold;
-        k.render_depth = false;
-        sh.s_sc[warp] = TraceScene{reinterpret_cast<const float4 *>(bs.geom), reinterpret_cast<const float4 *>(bs.l2w),
-                                   reinterpret_cast<const float2 *>(bs.live), vw.channels,
-                                   reinterpret_cast<const float4 *>(bs.nodes), bs.root_box, bs.n};
-    }
-    __syncwarp();
-    const TraceScene &sc = sh.s_sc[warp];
-    const TraceKnobs &k = sh.s_k[warp];
-    const HitSink hs{nullptr, nullptr, 0};
-    f3 ro = mk3(vw.origin[0], vw.origin[1], vw.origin[2]);
-    f3 rd = mk3(0.0f, 0.0f, 0.0f);
-    if (inside) rd = camera_ray(vw.w2c, vw.fov_y, px, py, vw.width, vw.height, 0.0f, 0.0f);
-    {
-        const int x0 = (int)((local % tiles_x) * tile_w), y0 = (int)((local / tiles_x) * tile_h);
-        make_frustum_warp(sh.sfr[warp], ro, vw.w2c, vw.fov_y, x0, y0, x0 + tile_w - 1, y0 + tile_h - 1, vw.width,
-                          vw.height, sh.s_sc[warp].root_box);
-    }
-    RayResult r;
-    trace_ray<KB, LO>(sc, k, ro, rd, inside, false, hs, status, sh.kbuf, r, &sh.sfr[warp], sh.sstk[warp],
-                      sh.scand[warp], &sh.scc[warp], front_base, front_off);
-    if (!inside) return;
-    float r0, r1, r2;
-    finish_ray(r, bs.bg, 1e-12f, false, r0, r1, r2);
-    float *o = out + vw.out_offset + 3 * ((size_t)py * vw.width + px);
-    o[0] = r.C0;
-    o[1] = r.C1;
-    o[2] = r.C2;
-}
-
 template <int KB, int MINB>
 __global__ void __launch_bounds__(kFwdThreads, MINB)
     trace_batch_kernel(const gray_batch_scene *__restrict__ scenes, const gray_batch_view *__restrict__ views,
                        int nviews, uint32_t total_packets, float *__restrict__ out, uint32_t *__restrict__ counter,
                        int tile_w, const uint32_t *__restrict__ frontier, uint32_t total_groups,
                        int32_t *status) {
-    __shared__ BatchShared<KB> sh;
-    const int lane = threadIdx.x & 31;
+    __shared__ unsigned long long kbuf[KB][kFwdThreads];
+    __shared__ Frustum sfr[kWarps];
+    __shared__ uint32_t sstk[kWarps][kWideStack];
+    __shared__ uint32_t scand[kWarps][kQueue];
+    __shared__ CandCache scc[kWarps];
+    // the packet's scene and view parameters live in shared memory (read where used), which keeps
+    // them out of the registers the traversal needs
+    __shared__ TraceScene s_sc[kWarps];
+    __shared__ TraceKnobs s_k[kWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tile_h = 32 / tile_w;
     for (;;) {
         __syncwarp();
         uint32_t packet = 0;
@@ -1661,11 +1607,39 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
         packet = __shfl_sync(kFull, packet, 0);
         if (packet >= total_packets) break;
         const gray_batch_view &vw = views[batch_view_of(views, nviews, packet)];
+        const gray_batch_scene &bs = scenes[vw.scene];
         const uint32_t local = packet - vw.packet_offset;
+        const uint32_t tiles_x = (vw.width + tile_w - 1) / tile_w;
+        const int px = (int)((local % tiles_x) * tile_w) + lane % tile_w;
+        const int py = (int)((local / tiles_x) * tile_h) + lane / tile_w;
+        const bool inside = px < (int)vw.width && py < (int)vw.height;
+        if (lane == 0) {
+            TraceKnobs &k = s_k[warp];
+            k.znear = vw.znear;
+            k.zfar = vw.zfar;
+            k.athr = bs.alpha_threshold;
+            k.pw = bs.exp_power;
+            k.tthr = bs.t_threshold;
+            k.render_depth = false;
+            s_sc[warp] = TraceScene{reinterpret_cast<const float4 *>(bs.geom), reinterpret_cast<const float4 *>(bs.l2w),
+                                    reinterpret_cast<const float2 *>(bs.live), vw.channels,
+                                    reinterpret_cast<const float4 *>(bs.nodes), bs.root_box, bs.n};
+        }
+        __syncwarp();
+        const TraceScene &sc = s_sc[warp];
+        const TraceKnobs &k = s_k[warp];
+        const HitSink hs{nullptr, nullptr, 0};
+        f3 ro = mk3(vw.origin[0], vw.origin[1], vw.origin[2]);
+        f3 rd = mk3(0.0f, 0.0f, 0.0f);
+        if (inside) rd = camera_ray(vw.w2c, vw.fov_y, px, py, vw.width, vw.height, 0.0f, 0.0f);
+        {
+            const int x0 = (int)((local % tiles_x) * tile_w), y0 = (int)((local / tiles_x) * tile_h);
+            make_frustum_warp(sfr[warp], ro, vw.w2c, vw.fov_y, x0, y0, x0 + tile_w - 1, y0 + tile_h - 1, vw.width,
+                              vw.height, s_sc[warp].root_box);
+        }
         const uint32_t *front = nullptr;
         uint32_t front_off = 0u;
         if (frontier) {
-            const uint32_t tiles_x = (vw.width + tile_w - 1) / tile_w;
             const uint32_t tx = local % tiles_x, ty = local / tiles_x;
             const uint32_t grp = vw.group_offset + (ty / 2) * ((tiles_x + 1) / 2) + tx / 2;
             if (grp < total_groups) {  // else: from the root
@@ -1673,37 +1647,16 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
                 front_off = grp * (uint32_t)kFrontierWords;
             }
         }
-        batch_packet<KB, (MINB < 6)>(scenes, vw, local, tile_w, out, front, front_off, status, sh);
-    }
-}
-
-// Group mode (variant bit 6): a block takes one 2x2 packet group at a time from the counter and its
-// four warps trace the group's four packets side by side, as the plain forward's blocks do with a
-// pixel tile, so the group's frontier and the nodes and Gaussians its packets share stay in one L1.
-template <int KB, int MINB>
-__global__ void __launch_bounds__(kFwdThreads, MINB)
-    trace_batch_group_kernel(const gray_batch_scene *__restrict__ scenes, const gray_batch_view *__restrict__ views,
-                             int nviews, float *__restrict__ out, uint32_t *__restrict__ counter, int tile_w,
-                             const uint32_t *__restrict__ frontier, uint32_t total_groups, int32_t *status) {
-    __shared__ BatchShared<KB> sh;
-    __shared__ uint32_t s_group;
-    const int warp = threadIdx.x >> 5;
-    const int tile_h = 32 / tile_w;
-    for (;;) {
-        __syncthreads();  // every warp is done with the previous group
-        if (threadIdx.x == 0) s_group = atomicAdd(counter, 1u);
-        __syncthreads();
-        const uint32_t group = s_group;
-        if (group >= total_groups) break;
-        int v = 0;
-        while (v + 1 < nviews && views[v + 1].group_offset <= group) v++;
-        const gray_batch_view &vw = views[v];
-        const uint32_t tiles_x = (vw.width + tile_w - 1) / tile_w, tiles_y = (vw.height + tile_h - 1) / tile_h;
-        const uint32_t gxn = (tiles_x + 1) / 2, lg = group - vw.group_offset;
-        const uint32_t tx = (lg % gxn) * 2 + (uint32_t)(warp & 1), ty = (lg / gxn) * 2 + (uint32_t)(warp >> 1);
-        if (tx < tiles_x && ty < tiles_y)
-            batch_packet<KB, (MINB < 6)>(scenes, vw, ty * tiles_x + tx, tile_w, out, frontier,
-                                         group * (uint32_t)kFrontierWords, status, sh);
+        RayResult r;
+        trace_ray<KB, (MINB < 6)>(sc, k, ro, rd, inside, false, hs, status, kbuf, r, &sfr[warp], sstk[warp], scand[warp],
+                      &scc[warp], front, front_off);
+        if (!inside) continue;
+        float r0, r1, r2;
+        finish_ray(r, bs.bg, 1e-12f, false, r0, r1, r2);
+        float *o = out + vw.out_offset + 3 * ((size_t)py * vw.width + px);
+        o[0] = r.C0;
+        o[1] = r.C1;
+        o[2] = r.C2;
     }
 }
 
@@ -1908,15 +1861,6 @@ cudaError_t launch_trace_batch(const gray_batch_scene *scenes, const gray_batch_
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     const uint32_t *fr = frontier;
-    if ((v & 64) && total_groups > 0) {  // group mode: blocks take 2x2 packet groups
-        switch (v & 3) {
-            case 0: trace_batch_group_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, out, counter, tile_w, fr, total_groups, status); break;
-            case 1: trace_batch_group_kernel<32, 4><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, out, counter, tile_w, fr, total_groups, status); break;
-            case 2: trace_batch_group_kernel<16, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, out, counter, tile_w, fr, total_groups, status); break;
-            default: trace_batch_group_kernel<16, 6><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, out, counter, tile_w, fr, total_groups, status); break;
-        }
-        return cudaGetLastError();
-    }
     switch (v & 3) {
         case 0: trace_batch_kernel<32, 1><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, total_groups, status); break;
         case 1: trace_batch_kernel<32, 4><<<grid, kFwdThreads, 0, s>>>(scenes, views, nviews, total_packets, out, counter, tile_w, fr, total_groups, status); break;

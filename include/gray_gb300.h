@@ -224,10 +224,8 @@ int gray_batch_prep(const gray_params *p, const float *origins, int32_t nviews, 
  * the launch resets and consumes; frontier is a device workspace of total_groups *
  * GRAY_FRONTIER_WORDS words (NULL: every traversal starts at the root) into which the launch first
  * writes each packet group's BVH frontier (a group index at or beyond total_groups, from an
- * inconsistent group_offset, starts at the root); variant as gray_params.trace_variant, and bit 6
- * (with total_groups > 0) has each block take a 2x2 packet group at a time, its four warps tracing
- * the group's packets side by side, instead of each warp taking single packets; blocks_per_sm sizes
- * the persistent grid (0 = 4). */
+ * inconsistent group_offset, starts at the root); variant as gray_params.trace_variant;
+ * blocks_per_sm sizes the persistent grid (0 = 4). */
 int gray_render_batch(const gray_batch_scene *scenes, const gray_batch_view *views, int32_t nviews,
                       uint32_t total_packets, float *out, uint32_t *work_counter, uint32_t *frontier,
                       uint32_t total_groups, int32_t variant, int32_t blocks_per_sm, int32_t *status,

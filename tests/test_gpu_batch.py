@@ -77,16 +77,3 @@ def test_request_alone_equals_request_in_mix():
     for k, req in enumerate(reqs):
         alone = BatchRenderer([ta, tb], use_graph=False, autotune=False, variant=3).render([req])[0]
         assert torch.equal(alone, mix[k])
-
-
-@pytest.mark.parametrize("variant", [1, 3, 5, 7, 64 + 1, 64 + 3, 64 + 5, 64 + 7])
-def test_batch_variants_and_group_mode_equal_plain(variant):
-    """Every batch kernel variant, packets claimed per warp or (bit 6) 2x2 packet groups claimed per
-    block, renders each view of a mixed batch exactly as the plain forward does."""
-    ta, tb = _scenes(128, 96)
-    tracers = [ta, tb]
-    reqs = _cams()
-    outs = [o.clone() for o in BatchRenderer(tracers, use_graph=False, autotune=False, variant=variant).render(reqs)]
-    torch.cuda.synchronize()
-    for (s, cam), got in zip(reqs, outs):
-        assert torch.equal(got, _plain(tracers[s], cam)), (variant, s, cam.image_width, cam.image_height)
