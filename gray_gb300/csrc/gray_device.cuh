@@ -280,31 +280,44 @@ __device__ __forceinline__ bool intersect_lo(const float4 m0, const float4 m1, c
     return true;
 }
 
-// The hit decision of intersect_lo() alone.
-__device__ __forceinline__ bool intersect_hits_lo(const float4 m0, const float4 m1, const float4 m2, float o, f3 rd,
-                                                  float alpha_threshold, float znear, float zfar) {
+// Division-free, conservative form of the hit decision of intersect() for the object-space ray
+// (lo, ld) with b = <lo, ld> as local_ray computes them: false only when intersect() on the same
+// lo, ld and b reports no hit (b > 0, or the max-density point outside the unit sphere); a true
+// may still be a miss.  The line's squared distance from the centre is |lo x ld|^2 / |ld|^2, and a
+// hit of intersect() puts it at most 1 + 5 ulp: its u is lo + t ld rounded, a point of the line.
+// The cross product's roundings are relative to |lo|_inf |ld| (linear, not quadratic, in |lo|), so
+// with q = 2^-24 |lo|_inf the computed C = |c|^2 stays below |ld|^2 (1 + 64 ulp + 4q + 4q^2) for
+// every hit; the range conditions keep every product finite and away from subnormals (outside them
+// the answer is true).  The all-pairs hit test of a packet runs this; the intersection program
+// (intersect, intersect_lo) decides, so results do not depend on it.
+__device__ __forceinline__ bool may_hit_local(f3 lo, f3 ld, float b) {
+    if (b > 0.0f) return false;
+    const float L = fdot3(ld, ld);
+    const float p0 = lo.z * ld.y, p1 = lo.x * ld.z, p2 = lo.y * ld.x;
+    const f3 c = mk3(fmaf(lo.y, ld.z, -p0), fmaf(lo.z, ld.x, -p1), fmaf(lo.x, ld.y, -p2));
+    const float C = fdot3(c, c);
+    const float li = fmaxf(fabsf(lo.x), fmaxf(fabsf(lo.y), fabsf(lo.z)));
+    const float q4 = li * 0x1.0p-22f;
+    const float k = fmaf(q4, fmaf(q4, 0.25f, 1.0f), 1.0f + 0x1.0p-18f);
+    return !(C > L * k && li <= 0x1.0p40f && L >= 0x1.0p-60f && L <= 0x1.0p40f);
+}
+
+// may_hit_local() for rows (M | lo) from local_origin, with the opacity test of intersect_lo().
+__device__ __forceinline__ bool may_hit_lo(const float4 m0, const float4 m1, const float4 m2, float o, f3 rd,
+                                           float alpha_threshold) {
     if (o <= alpha_threshold) return false;
     LocalHit h;
     local_ray_lo(m0, m1, m2, rd, h);
-    if (h.b > 0.0f) return false;
-    closest_point(h);
-    if (fdot3(h.u, h.u) > 1.0f) return false;
-    if (!(h.t >= znear && h.t <= zfar)) return unit_box_overlap(h, znear, zfar);
-    return true;
+    return may_hit_local(h.lo, h.ld, h.b);
 }
 
-// The hit decision of intersect() alone (same arithmetic, so the same answer), without the
-// Gaussian response.
-__device__ __forceinline__ bool intersect_hits(const float4 g0, const float4 g1, const float4 g2, float o, f3 ro,
-                                               f3 rd, float alpha_threshold, float znear, float zfar) {
+// may_hit_local() for snapshot rows (M | mu), with the opacity test of intersect().
+__device__ __forceinline__ bool may_hit(const float4 g0, const float4 g1, const float4 g2, float o, f3 ro, f3 rd,
+                                        float alpha_threshold) {
     if (o <= alpha_threshold) return false;
     LocalHit h;
     local_ray(g0, g1, g2, ro, rd, h);
-    if (h.b > 0.0f) return false;
-    closest_point(h);
-    if (fdot3(h.u, h.u) > 1.0f) return false;
-    if (!(h.t >= znear && h.t <= zfar)) return unit_box_overlap(h, znear, zfar);
-    return true;
+    return may_hit_local(h.lo, h.ld, h.b);
 }
 
 // Colour in 2^-24 fixed point (clamped to [-64, 64], so it fits 31 bits): the tail sums add

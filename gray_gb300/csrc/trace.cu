@@ -343,8 +343,9 @@ __device__ __forceinline__ bool frustum_ellipsoid(const Frustum &fr, const float
 // packet frustum and fetches its snapshot rows, live values and colour; the survivors are
 // compacted into the warp's shared-memory cache, each with its object-space ray origin (the
 // packet's rays share the origin, so it is computed once per candidate, not once per lane).  (2) Every lane runs the hit test of its own ray
-// against every cached candidate and keeps a 32-bit mask of its hits.  (3) The lanes walk their
-// masks together, one hit per lane per step, through the intersection program and the selection.
+// against every cached candidate and keeps a 32-bit mask of its possible hits (may_hit: division-free
+// and conservative, a superset of the hits).  (3) The lanes walk their masks together, one candidate
+// per lane per step, through the intersection program, which decides the hit, and the selection.
 // The order in which a lane sees its hits does not matter: the all-hit sums are order-independent
 // and the selection is by key.  LO: the cache keeps each candidate's object-space ray origin in
 // place of its mean (computed once by the fetching lane; saves 12 instructions per hit test but
@@ -394,11 +395,9 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
     if (want) {
         for (int j = 0; j < nc; j++) {
             if constexpr (LO) {
-                if (intersect_hits_lo(cc.g[j][0], cc.g[j][1], cc.g[j][2], __int_as_float(cc.c[j].w), rd, k.athr,
-                                      k.znear, k.zfar))
+                if (may_hit_lo(cc.g[j][0], cc.g[j][1], cc.g[j][2], __int_as_float(cc.c[j].w), rd, k.athr))
                     mask |= 1u << j;
-            } else if (intersect_hits(cc.g[j][0], cc.g[j][1], cc.g[j][2], __int_as_float(cc.c[j].w), ro, rd, k.athr,
-                                      k.znear, k.zfar)) {
+            } else if (may_hit(cc.g[j][0], cc.g[j][1], cc.g[j][2], __int_as_float(cc.c[j].w), ro, rd, k.athr)) {
                 mask |= 1u << j;
             }
         }
