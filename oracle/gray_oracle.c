@@ -695,6 +695,47 @@ static inline is_result intersect(const float *g, float o, float sf, const float
     return res;
 }
 
+/* Hit decision of intersect() for an object-space ray (lo, ld): b = <lo,ld> <= 0 and the
+ * max-density point inside the unit sphere (the range test, which only removes hits, left out). */
+static int hit_local(const float lo[3], const float ld[3]) {
+    const float b = fdot3(lo, ld);
+    if (b > 0.0f) return 0;
+    const float t = -b / fdot3(ld, ld);
+    const float u[3] = {fmaf(t, ld[0], lo[0]), fmaf(t, ld[1], lo[1]), fmaf(t, ld[2], lo[2])};
+    return !(fdot3(u, u) > 1.0f);
+}
+
+/* Restatement of the CUDA path's division-free pretest (may_hit_local): 0 means "certainly no
+ * hit".  Not part of the reference's algorithm: the kernels use it to skip pairs before the
+ * intersection program, so it must never reject a pair that hit_local() accepts. */
+static int may_hit_local(const float lo[3], const float ld[3]) {
+    const float b = fdot3(lo, ld);
+    if (b > 0.0f) return 0;
+    const float L = fdot3(ld, ld);
+    const float p0 = lo[2] * ld[1], p1 = lo[0] * ld[2], p2 = lo[1] * ld[0];
+    const float c[3] = {fmaf(lo[1], ld[2], -p0), fmaf(lo[2], ld[0], -p1), fmaf(lo[0], ld[1], -p2)};
+    const float C = fdot3(c, c);
+    const float li = fmaxf(fabsf(lo[0]), fmaxf(fabsf(lo[1]), fabsf(lo[2])));
+    const float q4 = li * 0x1.0p-22f;
+    const float k = fmaf(q4, fmaf(q4, 0.25f, 1.0f), 1.0f + 0x1.0p-18f);
+    return !(C > L * k && li <= 0x1.0p40f && L >= 0x1.0p-60f && L <= 0x1.0p40f);
+}
+
+int orc_pretest_check(int n, const float *lo, const float *ld, int64_t *counts) {
+    int64_t hits = 0, maybes = 0, violations = 0;
+    for (int i = 0; i < n; i++) {
+        const int h = hit_local(lo + 3 * (size_t)i, ld + 3 * (size_t)i);
+        const int m = may_hit_local(lo + 3 * (size_t)i, ld + 3 * (size_t)i);
+        hits += h;
+        maybes += m;
+        violations += h && !m;
+    }
+    counts[0] = hits;
+    counts[1] = maybes;
+    counts[2] = violations;
+    return violations != 0;
+}
+
 typedef struct {
     uint64_t *keys;
     size_t n, cap;

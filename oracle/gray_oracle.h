@@ -137,6 +137,11 @@ void orc_ellipsoids(int nrays, const float *ray_o, const float *ray_d, int n, co
 
 int orc_hardware_threads(void);
 
+/* Checker of the CUDA path's division-free hit pretest (not a reference routine): for n object-space
+ * rays (lo, ld; 3 floats each) counts the pairs the exact hit decision accepts (counts[0]), the pairs
+ * the pretest keeps (counts[1]) and the accepted pairs it would drop (counts[2]; returns counts[2] != 0). */
+int orc_pretest_check(int n, const float *lo, const float *ld, int64_t *counts);
+
 #ifdef __cplusplus
 }
 #endif

@@ -102,12 +102,22 @@ def lib():
         L.orc_ellipsoids.argtypes = [ctypes.c_int, F32P, F32P, ctypes.c_int, F32P, F32P, F32P, ctypes.c_float,
                                      ctypes.c_float, ctypes.c_float, F32P, F32P, F32P, I32P, ctypes.c_int]
         L.orc_hardware_threads.restype = ctypes.c_int
+        L.orc_pretest_check.argtypes = [ctypes.c_int, F32P, F32P, I64P]
         _lib = L
     return _lib
 
 
 def _f32(a):
     return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def pretest_check(lo, ld):
+    """(accepted, kept, dropped) pair counts of the exact hit decision and of the CUDA path's
+    division-free pretest on object-space rays lo, ld (n x 3)."""
+    lo, ld = _f32(lo).reshape(-1, 3), _f32(ld).reshape(-1, 3)
+    counts = np.zeros(3, dtype=np.int64)
+    lib().orc_pretest_check(len(lo), lo, ld, counts)
+    return tuple(int(c) for c in counts)
 
 
 @dataclass

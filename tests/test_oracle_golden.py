@@ -223,3 +223,44 @@ def test_refit_climb_reports_a_corrupt_parent_chain(oracle):
     child = int(internal[0])
     tree.int_parent[0] = child  # the root's parent is now its own child
     assert tree.refit_climb(aabb) & 4 == 4
+
+
+def _lines(rng, n, dist, lo_mag, ld_mag):
+    """Object-space rays (lo, ld) whose lines pass at distance `dist` from the centre."""
+    e = rng.standard_normal((n, 3))
+    e /= np.linalg.norm(e, axis=1, keepdims=True)
+    w = rng.standard_normal((n, 3))
+    w -= np.sum(w * e, axis=1, keepdims=True) * e
+    w /= np.linalg.norm(w, axis=1, keepdims=True)
+    along = np.sqrt(np.maximum(lo_mag ** 2 - dist ** 2, 0.0))[:, None]
+    lo = w * dist[:, None] - along * e
+    ld = e * ld_mag[:, None]
+    return lo.astype(np.float32), ld.astype(np.float32)
+
+
+def test_hit_pretest_never_drops_a_hit(oracle):
+    """The kernels' division-free pretest (cross product with a rounding margin) keeps every pair
+    the exact hit decision accepts: lines within 1e-3 and 1e-6 of the unit sphere's surface,
+    object-space origins from 1e-3 to 1e11 away, direction lengths from 1e-15 to 1e15, zero
+    components, infinities and NaNs.  At the benchmark's magnitudes it keeps almost nothing else."""
+    rng = np.random.default_rng(7)
+    n = 400_000
+    for spread, lo_exp, ld_exp in ((1e-3, (-3, 4), (-15, 15)), (1e-6, (-3, 4), (-1, 3)),
+                                   (1e-3, (4, 11), (-3, 3)), (3.0, (-3, 11), (-15, 15))):
+        dist = 1.0 + (rng.random(n) - 0.5) * 2 * spread if spread < 1 else rng.random(n) * spread
+        lo, ld = _lines(rng, n, dist, 10.0 ** rng.uniform(*lo_exp, n), 10.0 ** rng.uniform(*ld_exp, n))
+        ld[::13, 1] = 0.0
+        lo[::17, 2] = 0.0
+        accepted, kept, dropped = oracle.pretest_check(lo, ld)
+        assert dropped == 0, (spread, lo_exp, ld_exp)
+        assert accepted > n // 20
+    special = np.array([np.inf, -np.inf, np.nan, 1e-40, 0.0, 3e38], dtype=np.float32)
+    lo, ld = _lines(rng, 6 * 6 * 3, np.ones(108), np.full(108, 5.0), np.ones(108))
+    for i in range(108):
+        (lo if i % 2 else ld)[i, i % 3] = special[(i // 3) % 6]
+    assert oracle.pretest_check(lo, ld)[2] == 0
+    # magnitudes of the benchmark scene: |lo| 10-2000, |ld| 1-1000
+    dist = rng.random(n) * 2.0
+    lo, ld = _lines(rng, n, dist, 10.0 ** rng.uniform(1, 3.3, n), 10.0 ** rng.uniform(0, 3, n))
+    accepted, kept, dropped = oracle.pretest_check(lo, ld)
+    assert dropped == 0 and kept - accepted <= max(2, accepted // 1000)
