@@ -311,15 +311,6 @@ __device__ __forceinline__ bool may_hit_lo(const float4 m0, const float4 m1, con
     return may_hit_local(h.lo, h.ld, h.b);
 }
 
-// may_hit_local() for snapshot rows (M | mu), with the opacity test of intersect().
-__device__ __forceinline__ bool may_hit(const float4 g0, const float4 g1, const float4 g2, float o, f3 ro, f3 rd,
-                                        float alpha_threshold) {
-    if (o <= alpha_threshold) return false;
-    LocalHit h;
-    local_ray(g0, g1, g2, ro, rd, h);
-    return may_hit_local(h.lo, h.ld, h.b);
-}
-
 // Colour in 2^-24 fixed point (clamped to [-64, 64], so it fits 31 bits): the tail sums add
 // alpha16_fixed(a) * colour_fixed(c), an exact 64-bit product in 2^-48 units.
 __device__ __forceinline__ int colour_fixed(float c) {

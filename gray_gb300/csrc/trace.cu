@@ -347,10 +347,9 @@ __device__ __forceinline__ bool frustum_ellipsoid(const Frustum &fr, const float
 // and conservative, a superset of the hits).  (3) The lanes walk their masks together, one candidate
 // per lane per step, through the intersection program, which decides the hit, and the selection.
 // The order in which a lane sees its hits does not matter: the all-hit sums are order-independent
-// and the selection is by key.  LO: the cache keeps each candidate's object-space ray origin in
-// place of its mean (computed once by the fetching lane; saves 12 instructions per hit test but
-// needs registers, so the register-capped kernels keep the mean and recompute per lane).
-template <int KB, bool LO>
+// and the selection is by key.  The cache keeps each candidate's object-space ray origin in place of
+// its mean (computed once by the fetching lane with local_origin, the arithmetic of local_ray).
+template <int KB>
 __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool want,
                                                  bool first, LaneState &st, unsigned long long (*kbuf)[kFwdThreads],
                                                  const Frustum &fr, uint32_t *cand, CandCache &cc, int nc) {
@@ -371,12 +370,10 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
         cv = make_int4(colour_fixed(cp[0]), colour_fixed(cp[1]), colour_fixed(cp[2]), __float_as_int(lv.x));
         sfv = lv.y;
         keep = sc.l2w ? frustum_ellipsoid(fr, sc.l2w + 3 * (size_t)gid) : true;
-        if constexpr (LO) {
-            const f3 lo = local_origin(g0, g1, g2, ro);
-            g0.w = lo.x;
-            g1.w = lo.y;
-            g2.w = lo.z;
-        }
+        const f3 lo = local_origin(g0, g1, g2, ro);
+        g0.w = lo.x;
+        g1.w = lo.y;
+        g2.w = lo.z;
     }
     const uint32_t bal = __ballot_sync(kFull, keep);
     __syncwarp();  // every read of cand[] precedes the compacting writes
@@ -394,12 +391,8 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
     uint32_t mask = 0u;
     if (want) {
         for (int j = 0; j < nc; j++) {
-            if constexpr (LO) {
-                if (may_hit_lo(cc.g[j][0], cc.g[j][1], cc.g[j][2], __int_as_float(cc.c[j].w), rd, k.athr))
-                    mask |= 1u << j;
-            } else if (may_hit(cc.g[j][0], cc.g[j][1], cc.g[j][2], __int_as_float(cc.c[j].w), ro, rd, k.athr)) {
+            if (may_hit_lo(cc.g[j][0], cc.g[j][1], cc.g[j][2], __int_as_float(cc.c[j].w), rd, k.athr))
                 mask |= 1u << j;
-            }
         }
     }
     while (__any_sync(kFull, mask != 0u)) {
@@ -407,7 +400,7 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
             const int j = __ffs(mask) - 1;
             mask &= mask - 1u;
             const int4 c = cc.c[j];
-            on_leaf_data<KB, LO>(cand[j], cc.g[j][0], cc.g[j][1], cc.g[j][2],
+            on_leaf_data<KB, true>(cand[j], cc.g[j][0], cc.g[j][1], cc.g[j][2],
                                    make_float2(__int_as_float(c.w), cc.sf[j]), c.x, c.y, c.z, first, ro, rd, k, st,
                                    kbuf);
         }
@@ -424,7 +417,7 @@ __device__ __forceinline__ void flush_candidates(const TraceScene &sc, const Tra
 // of at the root: the frontier goes onto the stack with its first entry on top, and a frontier leaf
 // is queued when it is popped.  Returns false if the shared stack overflowed (the caller then
 // repeats the traversal per ray).
-template <int KB, bool LO>
+template <int KB>
 __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool want,
                                                  bool first, LaneState &st, unsigned long long (*kbuf)[kFwdThreads],
                                                  const Frustum &fr, uint32_t *stk, uint32_t *cand,
@@ -520,7 +513,7 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
         while (nc >= kCand || (draining && nc > 0)) {
             // process the first kCand queued leaves, then move the rest to the front
             const int take = nc < kCand ? nc : kCand;
-            flush_candidates<KB, LO>(sc, k, ro, rd, want, first, st, kbuf, fr, cand, cc, take);
+            flush_candidates<KB>(sc, k, ro, rd, want, first, st, kbuf, fr, cand, cc, take);
             const int rest = nc - take;
             const uint32_t r0 = lane < rest ? cand[kCand + lane] : 0u;
             const uint32_t r1 = lane + 32 < rest ? cand[kCand + 32 + lane] : 0u;
@@ -539,7 +532,7 @@ __device__ __forceinline__ bool traverse_frustum(const TraceScene &sc, const Tra
 // Trace the warp's 32 rays (one per lane; `alive` lanes only) through the scene: traversal,
 // selection, compositing (cuda/forward_pass.cu:6-151 minus the write-out).  Every lane of the
 // warp must call this together.
-template <int KB, bool LO>
+template <int KB>
 __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs &k, f3 ro, f3 rd, bool alive,
                                           bool grads, const HitSink &hs, int32_t *status,
                                           unsigned long long (*kbuf)[kFwdThreads], RayResult &res,
@@ -572,7 +565,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
         // ---------------- traversal ----------------
         bool per_ray = fr == nullptr;
         if (!per_ray &&
-            !traverse_frustum<KB, LO>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, *wcc, front_base, front_off,
+            !traverse_frustum<KB>(sc, k, ro, rd, want, first, st, kbuf, *fr, wstk, wcand, *wcc, front_base, front_off,
                                       status)) {
             // the frustum traversal gave up (stack overflow): discard what it gathered, trace per ray
             st.kcount = 0;
@@ -823,7 +816,7 @@ struct FwdShared {
 
 // Packet (wx, wy) of pixel tile (bx, by) (a tile is 2x2 packets of tile_w x tile_h pixels), traced
 // by the calling warp; front_base + front_off: the tile's BVH frontier (count, entries), or a null base.
-template <int KB, bool LO>
+template <int KB>
 __device__ __forceinline__ void forward_packet(const FwdArgs &a, int bx, int by, int wx, int wy,
                                                const uint32_t *front_base, uint32_t front_off, FwdShared<KB> &sh) {
     unsigned long long(*kbuf)[kFwdThreads] = sh.kbuf;
@@ -848,11 +841,9 @@ __device__ __forceinline__ void forward_packet(const FwdArgs &a, int bx, int by,
     // ---- ray generation (cuda/shaders.cu:76-88) ----
     f3 ro = mk3(0.0f, 0.0f, 0.0f), rd = mk3(0.0f, 0.0f, 0.0f);
     bool alive = false;
-    // LO: every lane holds the camera origin, inactive ones too (a packet's candidates get their
+    // every lane holds the camera origin, inactive ones too (a packet's candidates get their
     // object-space origin from whichever lane fetches them)
-    if constexpr (LO) {
-        if (!*a.rays_from_python) ro = mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]);
-    }
+    if (!*a.rays_from_python) ro = mk3(a.cam_origin[0], a.cam_origin[1], a.cam_origin[2]);
     if (inside) {
         if (*a.rays_from_python) {
             ro = mk3(a.ray_o[3 * pixel], a.ray_o[3 * pixel + 1], a.ray_o[3 * pixel + 2]);
@@ -879,7 +870,7 @@ __device__ __forceinline__ void forward_packet(const FwdArgs &a, int bx, int by,
                           y1, a.render_w, a.render_h, a.root_box);
     }
     RayResult r;
-    trace_ray<KB, LO>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sh.sstk[warp],
+    trace_ray<KB>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sh.sstk[warp],
                   sh.scand[warp], &sh.scc[warp], frustum ? front_base : nullptr, front_off);
 
     if (!inside) return;
@@ -922,7 +913,7 @@ __device__ __forceinline__ void forward_packet(const FwdArgs &a, int bx, int by,
 
 // One block's pixel tile (bx, by): its four packets, one per warp; the tile's frontier is copied
 // into shared memory once by the block.
-template <int KB, bool LO>
+template <int KB>
 __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, FwdShared<KB> &sh) {
     const int warp = threadIdx.x >> 5;
     {   // every thread of the block gets here together
@@ -934,7 +925,7 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
         if (threadIdx.x == 0) sh.front[0] = use ? cnt : kFrontierNone;
         __syncthreads();
     }
-    forward_packet<KB, LO>(a, bx, by, warp % kBlockWarpsX, warp / kBlockWarpsX, sh.front, 0u, sh);
+    forward_packet<KB>(a, bx, by, warp % kBlockWarpsX, warp / kBlockWarpsX, sh.front, 0u, sh);
 }
 
 // Grid launch: block (x, y) renders tile (x, y).
@@ -942,7 +933,7 @@ template <int KB, int MINB>
 __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const FwdArgs a) {
     __shared__ FwdShared<KB> sh;
     if (*a.render_ellipsoids) return;  // the ellipsoid view (ellipsoid_kernel) renders this frame
-    forward_tile<KB, (MINB < 6)>(a, blockIdx.x, blockIdx.y, sh);
+    forward_tile<KB>(a, blockIdx.x, blockIdx.y, sh);
 }
 
 // Persistent launch: the blocks take tiles from the schedule's order, densest first, until none is
@@ -959,7 +950,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_sched_kernel(
         const uint32_t t = s_next;
         if (t >= (uint32_t)a.ntiles) break;
         const uint32_t tile = a.schedule[kSchedHeader + a.ntiles + t];
-        forward_tile<KB, (MINB < 6)>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x), sh);
+        forward_tile<KB>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x), sh);
     }
 }
 
@@ -978,7 +969,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_claim_kernel(
         q = __shfl_sync(kFull, q, 0);
         if (q >= (uint32_t)kWarps * (uint32_t)a.ntiles) break;
         const uint32_t tile = a.schedule[kSchedHeader + a.ntiles + q / kWarps], sub = q % kWarps;
-        forward_packet<KB, (MINB < 6)>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x),
+        forward_packet<KB>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x),
                                        (int)(sub % kBlockWarpsX), (int)(sub / kBlockWarpsX), a.frontier,
                                        tile * (uint32_t)kFrontierWords, sh);
     }
@@ -1647,7 +1638,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
             }
         }
         RayResult r;
-        trace_ray<KB, (MINB < 6)>(sc, k, ro, rd, inside, false, hs, status, kbuf, r, &sfr[warp], sstk[warp], scand[warp],
+        trace_ray<KB>(sc, k, ro, rd, inside, false, hs, status, kbuf, r, &sfr[warp], sstk[warp], scand[warp],
                       &scc[warp], front, front_off);
         if (!inside) continue;
         float r0, r1, r2;
