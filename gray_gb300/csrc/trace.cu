@@ -321,8 +321,10 @@ __device__ __forceinline__ bool frustum_box(const Frustum &fr, const float bmin[
 // Conservative frustum test of a Gaussian's support ellipsoid {mu + L u : |u| <= 1} (L, mu = the
 // snapshot's l2w rows): false only when the ellipsoid lies outside one plane by more than a rounding
 // margin.  The ellipsoid's extent along a normal n is |L^T n| (taken 3e-5 larger for its own
-// rounding).  A ray can only hit a Gaussian whose ellipsoid it crosses, so a leaf whose ellipsoid
-// misses the packet's frustum holds no hit of the packet even when its box passed.
+// rounding), compared squared with the gap between the plane's threshold and the centre's signed
+// distance (no square root; a gap that is not positive, an infinite extent or a NaN never culls).
+// A ray can only hit a Gaussian whose ellipsoid it crosses, so a leaf whose ellipsoid misses the
+// packet's frustum holds no hit of the packet even when its box passed.
 __device__ __forceinline__ bool frustum_ellipsoid(const Frustum &fr, const float4 *l2w) {
     const float4 r0 = l2w[0], r1 = l2w[1], r2 = l2w[2];
 #pragma unroll
@@ -332,8 +334,8 @@ __device__ __forceinline__ bool frustum_ellipsoid(const Frustum &fr, const float
         const float e0 = fmaf(r2.x, n.z, fmaf(r1.x, n.y, r0.x * n.x));
         const float e1 = fmaf(r2.y, n.z, fmaf(r1.y, n.y, r0.y * n.x));
         const float e2 = fmaf(r2.z, n.z, fmaf(r1.z, n.y, r0.z * n.x));
-        const float ext = sqrtf(fmaf(e2, e2, fmaf(e1, e1, e0 * e0)));
-        if (fmaf(ext, 1.00003f, sd) < fr.pa[p].w) return false;
+        const float gap = fr.pa[p].w - sd;
+        if (gap > 0.0f && fmaf(e2, e2, fmaf(e1, e1, e0 * e0)) * 1.00006f < gap * gap) return false;
     }
     return true;
 }
