@@ -465,6 +465,57 @@ def test_znear_zfar_and_render_rectangle(oracle):
     assert all(len(lists[i]) == 0 for i in np.nonzero(~mask.ravel())[0])
 
 
+def test_grazing_rays_at_the_support_sphere_match_the_oracle(oracle):
+    """Camera rays that pass within 2e-4 (relative) of their Gaussian's support sphere, on both
+    sides: the packets' division-free hit pretest must keep every pair the intersection program
+    accepts, so hit counts, lists and images stay bit-identical to the oracle."""
+    W, H = 64, 48
+    n = W * H
+    rot = np.tile(np.array([1.0, 0.0, 0.0, 0.0], np.float32), (n, 1))
+    scale = np.full((n, 3), math.log(0.02), np.float32)
+    opac = np.full((n, 1), 2.0, np.float32)
+    cam = synthetic.look_at((0.0, -5.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 0.9, W, H)
+
+    def render(mean, chan):
+        rt = G.make_tracer(W, H, mean, rot, scale, opac, channels=chan)
+        c = rt.get_camera()
+        c.vertical_fov_radians.fill_(cam.fov_y)
+        c.set_pose(cam.origin_cuda(), cam.rotation_c2w_blender_cuda())
+        rt.get_config().rays_from_python.fill_(False)
+        with torch.enable_grad():
+            rt.forward_pass()
+        torch.cuda.synchronize()
+        rt.check_status()
+        return rt
+
+    rng = np.random.default_rng(11)
+    chan = rng.uniform(0.0, 1.0, (n, 3)).astype(np.float32)
+    f0 = G.fb_numpy(render(rng.uniform(-1.0, 1.0, (n, 3)).astype(np.float32), chan))
+    ro, rd = f0["ray_origin"].astype(np.float64), f0["ray_direction"].astype(np.float64)
+    radius = 1.0 / float(oracle.snapshot(np.zeros((1, 3), np.float32), rot[:1], scale[:1], opac[:, 0][:1], 0.01)[0][0, 0])
+    side = rng.standard_normal((n, 3))
+    side -= np.sum(side * rd, axis=1, keepdims=True) * rd / np.sum(rd * rd, axis=1, keepdims=True)
+    side /= np.linalg.norm(side, axis=1, keepdims=True)
+    eps = rng.uniform(-2e-4, 2e-4, n)
+    mean = (ro + rng.uniform(3.5, 6.5, (n, 1)) * rd + (radius * (1.0 + eps))[:, None] * side).astype(np.float32)
+
+    rt = render(mean, chan)
+    f = G.fb_numpy(rt)
+    assert np.array_equal(f["ray_direction"], f0["ray_direction"])
+    geom, l2w, aabb, vis, live = _oracle_scene(oracle, mean, rot, scale, opac)
+    fwd = oracle.trace_forward(f["ray_origin"], f["ray_direction"], geom, live, chan, vis,
+                               oracle.TraceConfig(t_threshold=0.03))
+    _compare_forward(rt, fwd)
+    # the pixels' own Gaussians: the line's distance from the centre, in support radii (float64)
+    rel = ro - mean.astype(np.float64)
+    cross = np.cross(rel, rd)
+    dist = np.linalg.norm(cross, axis=1) / np.linalg.norm(rd, axis=1) / radius
+    assert np.count_nonzero(np.abs(dist - 1.0) < 2e-5) > 150
+    lists = G.hit_lists(rt)
+    own = np.array([i in set(lists[i].tolist()) for i in range(n)])
+    assert own[dist < 1.0 - 5e-5].all() and not own[dist > 1.0 + 5e-5].any()
+
+
 def test_inactive_pixels_and_empty_scene(oracle):
     sc = synthetic.small_scene(seed=1, n=16)
     chan = np.ones((sc.n, 3), np.float32)
