@@ -7,9 +7,9 @@
 //   every packet traversal starts there.  The packet traverses as a frustum: each step pops up to
 //   32 nodes (one per lane) from a per-warp shared-memory stack, tests both child boxes against the
 //   frustum, pushes the nearer child last and queues leaves; queued leaves are culled by an exact
-//   ellipsoid-frustum test, cached in shared memory, hit-tested by every lane against its own ray,
-//   and the lanes then walk their hit masks through the intersection program of
-//   cuda/shaders.cu:10-67.  The first traversal accumulates, over ALL hits, the full transmittance
+//   ellipsoid-frustum test, cached in shared memory, tested by every lane against its own ray with a
+//   division-free conservative pretest, and the lanes then walk their masks of possible hits through
+//   the intersection program of cuda/shaders.cu:10-67, which decides each hit.  The first traversal accumulates, over ALL hits, the full transmittance
 //   (an order-independent fixed-point sum of log(1 - alpha)) and the alpha-weighted colour sums of
 //   the reference's truncated-tail estimate, and every traversal keeps the KB nearest hits above a
 //   resume key in a per-lane shared-memory buffer of 64-bit keys (fp16 distance | gaussian id |
