@@ -77,7 +77,9 @@ def test_reference_scenes_forward_backward(oracle, golden, name):
     fwd = oracle.trace_forward(golden["rays_o"], golden["rays_d"], geom, live, golden[p + "color"], vis, cfg)
     _compare_forward(rt, fwd)
     img = G.fb_numpy(rt)["output_channels"]
-    assert np.abs(img - golden[p + "ref64_rgb"]).max() < 3e-4  # fp16-alpha bound vs the FP64 test loop
+    err = np.abs(img - golden[p + "ref64_rgb"]).astype(np.float64)
+    assert err.max() < 3e-4  # fp16-alpha bound vs the FP64 test loop
+    assert 10.0 * math.log10(1.0 / np.mean(err ** 2)) >= 60.0  # PSNR, peak 1
 
     gout = golden[p + "ref64_grad_out"]
     rt.get_framebuffer().grad_output_channels.copy_(torch.from_numpy(gout).reshape(32, 32, 3))
