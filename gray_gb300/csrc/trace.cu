@@ -322,7 +322,8 @@ __device__ __forceinline__ bool frustum_box(const Frustum &fr, const float bmin[
 // snapshot's l2w rows): false only when the ellipsoid lies outside one plane by more than a rounding
 // margin.  The ellipsoid's extent along a normal n is |L^T n| (taken 3e-5 larger for its own
 // rounding), compared squared with the gap between the plane's threshold and the centre's signed
-// distance (no square root; a gap that is not positive, an infinite extent or a NaN never culls).
+// distance (no square root; a gap below 2^-60, so that its square stays a normal float, an
+// infinite extent or a NaN never culls).
 // A ray can only hit a Gaussian whose ellipsoid it crosses, so a leaf whose ellipsoid misses the
 // packet's frustum holds no hit of the packet even when its box passed.
 __device__ __forceinline__ bool frustum_ellipsoid(const Frustum &fr, const float4 *l2w) {
@@ -335,7 +336,7 @@ __device__ __forceinline__ bool frustum_ellipsoid(const Frustum &fr, const float
         const float e1 = fmaf(r2.y, n.z, fmaf(r1.y, n.y, r0.y * n.x));
         const float e2 = fmaf(r2.z, n.z, fmaf(r1.z, n.y, r0.z * n.x));
         const float gap = fr.pa[p].w - sd;
-        if (gap > 0.0f && fmaf(e2, e2, fmaf(e1, e1, e0 * e0)) * 1.00006f < gap * gap) return false;
+        if (gap > 0x1.0p-60f && fmaf(e2, e2, fmaf(e1, e1, e0 * e0)) * 1.00006f < gap * gap) return false;
     }
     return true;
 }

@@ -721,6 +721,41 @@ static int may_hit_local(const float lo[3], const float ld[3]) {
     return !(C > L * k && li <= 0x1.0p40f && L >= 0x1.0p-60f && L <= 0x1.0p40f);
 }
 
+/* Restatement of the CUDA path's ellipsoid-plane cull (frustum_ellipsoid, one plane): 1 means
+ * "the ellipsoid {mu + L u : |u| <= 1} lies below the threshold w along n" (the packet's rays cannot
+ * reach it).  Not part of the reference's algorithm: a checker of the cull's rounding margin. */
+static int ellipsoid_plane_cull(const float n[3], const float *l2w, float w) {
+    const float *r0 = l2w, *r1 = l2w + 4, *r2 = l2w + 8;
+    const float sd = fmaf(n[2], r2[3], fmaf(n[1], r1[3], n[0] * r0[3]));
+    const float e0 = fmaf(r2[0], n[2], fmaf(r1[0], n[1], r0[0] * n[0]));
+    const float e1 = fmaf(r2[1], n[2], fmaf(r1[1], n[1], r0[1] * n[0]));
+    const float e2 = fmaf(r2[2], n[2], fmaf(r1[2], n[1], r0[2] * n[0]));
+    const float gap = w - sd;
+    return gap > 0x1.0p-60f && fmaf(e2, e2, fmaf(e1, e1, e0 * e0)) * 1.00006f < gap * gap;
+}
+
+int orc_cull_check(int n, const float *normals, const float *l2w, const float *thresholds, const double *planes,
+                   int64_t *counts) {
+    int64_t culled = 0, wrong = 0;
+    for (int i = 0; i < n; i++) {
+        const float *nn = normals + 3 * (size_t)i, *g = l2w + 12 * (size_t)i;
+        if (!ellipsoid_plane_cull(nn, g, thresholds[i])) continue;
+        culled++;
+        /* exact: the ellipsoid's highest point along n is n.mu + |L^T n| */
+        double sd = 0.0, ext = 0.0;
+        for (int r = 0; r < 3; r++) sd += (double)nn[r] * (double)g[4 * r + 3];
+        for (int c = 0; c < 3; c++) {
+            double e = 0.0;
+            for (int r = 0; r < 3; r++) e += (double)g[4 * r + c] * (double)nn[r];
+            ext += e * e;
+        }
+        if (!(sd + sqrt(ext) < planes[i])) wrong++;
+    }
+    counts[0] = culled;
+    counts[1] = wrong;
+    return wrong != 0;
+}
+
 int orc_pretest_check(int n, const float *lo, const float *ld, int64_t *counts) {
     int64_t hits = 0, maybes = 0, violations = 0;
     for (int i = 0; i < n; i++) {

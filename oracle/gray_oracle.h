@@ -142,6 +142,13 @@ int orc_hardware_threads(void);
  * the pretest keeps (counts[1]) and the accepted pairs it would drop (counts[2]; returns counts[2] != 0). */
 int orc_pretest_check(int n, const float *lo, const float *ld, int64_t *counts);
 
+/* Checker of the CUDA path's ellipsoid-plane cull (not a reference routine): for n planes (normals,
+ * 3 floats each; the cull's thresholds w, which hold the plane's rounding margin; the planes' exact
+ * offsets) and ellipsoids (l2w rows, 12 floats each) counts the culls (counts[0]) and the culls that
+ * FP64 says are wrong, the ellipsoid reaching the plane (counts[1]; returns counts[1] != 0). */
+int orc_cull_check(int n, const float *normals, const float *l2w, const float *thresholds, const double *planes,
+                   int64_t *counts);
+
 #ifdef __cplusplus
 }
 #endif

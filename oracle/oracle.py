@@ -103,6 +103,7 @@ def lib():
                                      ctypes.c_float, ctypes.c_float, F32P, F32P, F32P, I32P, ctypes.c_int]
         L.orc_hardware_threads.restype = ctypes.c_int
         L.orc_pretest_check.argtypes = [ctypes.c_int, F32P, F32P, I64P]
+        L.orc_cull_check.argtypes = [ctypes.c_int, F32P, F32P, F32P, F64P, I64P]
         _lib = L
     return _lib
 
@@ -117,6 +118,17 @@ def pretest_check(lo, ld):
     lo, ld = _f32(lo).reshape(-1, 3), _f32(ld).reshape(-1, 3)
     counts = np.zeros(3, dtype=np.int64)
     lib().orc_pretest_check(len(lo), lo, ld, counts)
+    return tuple(int(c) for c in counts)
+
+
+def cull_check(normals, l2w, thresholds, planes):
+    """(culled, wrong) counts of the CUDA path's ellipsoid-plane cull against FP64 on n planes
+    (normals n x 3, the cull's thresholds n, the planes' exact offsets n) and ellipsoids (l2w rows
+    n x 12)."""
+    normals, l2w, thresholds = _f32(normals).reshape(-1, 3), _f32(l2w).reshape(-1, 12), _f32(thresholds).reshape(-1)
+    planes = np.ascontiguousarray(planes, dtype=np.float64).reshape(-1)
+    counts = np.zeros(2, dtype=np.int64)
+    lib().orc_cull_check(len(normals), normals, l2w, thresholds, planes, counts)
     return tuple(int(c) for c in counts)
 
 

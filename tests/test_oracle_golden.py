@@ -266,3 +266,39 @@ def test_hit_pretest_never_drops_a_hit(oracle):
     lo, ld = _lines(rng, n, dist, 10.0 ** rng.uniform(1, 3.3, n), 10.0 ** rng.uniform(0, 3, n))
     accepted, kept, dropped = oracle.pretest_check(lo, ld)
     assert dropped == 0 and kept - accepted <= max(2, accepted // 1000)
+
+
+def test_ellipsoid_cull_never_culls_a_reachable_ellipsoid(oracle):
+    """The kernels' ellipsoid-plane cull (squared extent against the squared gap, 6e-5 margin, gaps
+    below 2^-60 never culled), given the frustum plane's threshold with its rounding margin
+    (1e-5 |n|_1 (3m + |o|_1), m bounding the coordinates), culls only ellipsoids that FP64 puts
+    entirely below the plane: planes within 1e-4 (relative) of the ellipsoid's top on both sides,
+    extents from 1e-25 to 1e15, scenes of 1e-20 (subnormal squares), scaled normals, and degenerate
+    (flat) ellipsoids."""
+    rng = np.random.default_rng(3)
+    n = 300_000
+    for ext_exp, mu_exp, near in (((-3, 1), (-3, 3), 1e-4), ((-25, -15), (-3, 3), 1e-4), ((5, 15), (-3, 3), 1e-4),
+                                  ((-25, 15), (-3, 3), 0.5), ((-25, -20), (-24, -20), 1e-4)):
+        q = rng.standard_normal((n, 4))
+        q /= np.linalg.norm(q, axis=1, keepdims=True)
+        w_, x, y, z = q.T
+        R = np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w_ * z), 2 * (x * z + w_ * y)], -1),
+                      np.stack([2 * (x * y + w_ * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w_ * x)], -1),
+                      np.stack([2 * (x * z - w_ * y), 2 * (y * z + w_ * x), 1 - 2 * (x * x + y * y)], -1)], 1)
+        s = 10.0 ** rng.uniform(*ext_exp, (n, 3))
+        s[::7, 2] = 0.0                                   # flat ellipsoids
+        L = R * s[:, None, :]
+        mu = rng.standard_normal((n, 3)) * 10.0 ** rng.uniform(*mu_exp, (n, 1))
+        nrm = rng.standard_normal((n, 3)) * 10.0 ** rng.uniform(-2, 2, (n, 1))
+        l2w = np.concatenate([L, mu[:, :, None]], axis=2).reshape(n, 12).astype(np.float32)
+        L32, mu32, n32 = l2w.reshape(n, 3, 4)[:, :, :3].astype(np.float64), l2w.reshape(n, 3, 4)[:, :, 3].astype(
+            np.float64), nrm.astype(np.float32).astype(np.float64)
+        top = np.sum(n32 * mu32, axis=1) + np.linalg.norm(np.einsum("nrc,nr->nc", L32, n32), axis=1)
+        scale = np.abs(top) + np.linalg.norm(np.einsum("nrc,nr->nc", L32, n32), axis=1)
+        plane = top + rng.uniform(-near, near, n) * scale
+        m = np.max(np.abs(mu32), axis=1) + np.max(np.abs(L32), axis=(1, 2)) * 3.0
+        mell = 1e-5 * np.sum(np.abs(n32), axis=1) * 3.0 * m + 1e-30
+        thr = (plane.astype(np.float32) - mell.astype(np.float32)).astype(np.float32)
+        culled, wrong = oracle.cull_check(nrm, l2w, thr, plane)
+        assert wrong == 0, (ext_exp, mu_exp, near, culled, wrong)
+        assert culled > n // 50 or mu_exp[1] < -15  # (tiny scenes: gaps below 2^-60 are never culled)
