@@ -77,3 +77,46 @@ def test_request_alone_equals_request_in_mix():
     for k, req in enumerate(reqs):
         alone = BatchRenderer([ta, tb], use_graph=False, autotune=False, variant=3).render([req])[0]
         assert torch.equal(alone, mix[k])
+
+
+def test_grazing_rays_batched_equal_plain_for_every_candidate_variant():
+    """One Gaussian per pixel whose support sphere the pixel's camera ray grazes (within 2e-4,
+    both sides): every kernel variant the autotuner may pick renders it in the batch kernel with
+    exactly the bits of the plain path (whose hit lists equal the oracle's on the same scene)."""
+    import math
+
+    from gray_gb300.batch import TUNE_CANDIDATES
+
+    W, H = 64, 48
+    n = W * H
+    rot = np.tile(np.array([1.0, 0.0, 0.0, 0.0], np.float32), (n, 1))
+    scale = np.full((n, 3), math.log(0.02), np.float32)
+    opac = np.full((n, 1), 2.0, np.float32)
+    cam = synthetic.look_at((0.0, -5.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 0.9, W, H)
+    rng = np.random.default_rng(12)
+    chan = rng.uniform(0.0, 1.0, (n, 3)).astype(np.float32)
+    probe = G.make_tracer(W, H, rng.uniform(-1.0, 1.0, (n, 3)).astype(np.float32), rot, scale, opac, channels=chan)
+    c = probe.get_camera()
+    c.vertical_fov_radians.fill_(cam.fov_y)
+    c.set_pose(cam.origin_cuda(), cam.rotation_c2w_blender_cuda())
+    probe.get_config().rays_from_python.fill_(False)
+    with torch.enable_grad():
+        probe.forward_pass()
+    torch.cuda.synchronize()
+    f = G.fb_numpy(probe)
+    ro, rd = f["ray_origin"].astype(np.float64), f["ray_direction"].astype(np.float64)
+    radius = 0.02 * math.sqrt(math.sqrt(4.0 * math.log((1.0 / (1.0 + math.exp(-2.0))) / 0.01)))
+    side = rng.standard_normal((n, 3))
+    side -= np.sum(side * rd, axis=1, keepdims=True) * rd / np.sum(rd * rd, axis=1, keepdims=True)
+    side /= np.linalg.norm(side, axis=1, keepdims=True)
+    eps = rng.uniform(-2e-4, 2e-4, n)
+    mean = (ro + rng.uniform(3.5, 6.5, (n, 1)) * rd + (radius * (1.0 + eps))[:, None] * side).astype(np.float32)
+    tracer = G.make_tracer(W, H, mean, rot, scale, opac, channels=chan)
+    ref = _plain(tracer, cam)
+    assert ref.abs().sum().item() > 0
+    for variant, bps in TUNE_CANDIDATES:
+        br = BatchRenderer([tracer], use_graph=False, autotune=False, variant=variant, blocks_per_sm=bps)
+        got = br.render([(0, cam)])[0].clone()
+        torch.cuda.synchronize()
+        br.check_status()
+        assert torch.equal(got, ref), (variant, bps, (got - ref).abs().max().item())
