@@ -434,16 +434,18 @@ def gpu_arm(a, rank, world, local_rank):
     peak, peak_kind = measured_peak_gbs()
     achieved = algo.get(dominant, 0.0) / (dom_ms / 1000.0) / 1e9
     # kernels behind one profiled scope: adam = step count + update; trace_backward = backward
-    # record + replay; tile_schedule = tile work estimate + bucket scan + scatter (on the library's
-    # side stream, beside forward_prep), then trace_forward = the trace (all four in trace_forward
+    # record + replay; tile_schedule = super-tile walk + tile walk + bucket scan + scatter (on the
+    # library's side stream, beside forward_prep), then trace_forward = the trace: with the default
+    # variant the narrow and the wide kernel, one of which returns at once (all in trace_forward
     # when no side stream could be had); refit = block-local climb + upper tree.  The snapshot, the
     # forward preparation and the backward record run a bulk-copy kernel over whole tiles (128, 64
     # and 128 Gaussians) and a plain one over the rest.
     def tiled(tile):
         return int(n >= tile) + int(n % tile != 0)
 
-    kernels_per_group = {"adam": 2, "trace_backward": 1 + tiled(128), "refit": 2, "tile_schedule": 3,
-                         "trace_forward": 1 if "tile_schedule" in res else 4, "snapshot": tiled(128),
+    traces = 2 if not a.trace_variant else 1
+    kernels_per_group = {"adam": 2, "trace_backward": 1 + tiled(128), "refit": 2, "tile_schedule": 4,
+                         "trace_forward": traces if "tile_schedule" in res else 4 + traces, "snapshot": tiled(128),
                          "forward_prep": tiled(64)}
     launches = sum(cnt * kernels_per_group.get(name, 1) for name, (_, cnt) in res.items())
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

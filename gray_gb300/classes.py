@@ -333,7 +333,7 @@ class Raytracer:
         # work order of the forward's pixel tiles (densest first), rebuilt by every forward
         self.schedule = torch.zeros(int(_lib.load().gray_schedule_words(self.width, self.height)), device=dev,
                                     dtype=torch.int32)
-        self.trace_variant = 0  # forward-kernel variant (0 = library default); results do not depend on it
+        self.trace_variant = 0  # forward-kernel variant (0 = automatic choice); results do not depend on it
         # counts forwards: each one overwrites the colours, saved state and hit lists a backward replays
         self.generation = 0
         self._scene = _SceneWorkspace(1, dev, not self.inference_only)
@@ -417,7 +417,7 @@ class Raytracer:
         self._invalidate()
 
     def set_trace_variant(self, variant: int):
-        """Select the forward-trace kernel variant (0 = default); every variant gives identical
+        """Select the forward-trace kernel variant (0 = automatic choice); every variant gives identical
         results."""
         self.trace_variant = int(variant)
         self._invalidate()

@@ -41,6 +41,19 @@ constexpr int kWideStack = 256;  // per-warp shared stack of the frustum travers
 constexpr int kCand = 32;        // leaves processed per flush (one per lane)
 constexpr int kQueue = 3 * kCand; // per-warp queue of leaves: < kCand before a step, + up to 64 per step
 constexpr int kSchedHeader = 64;  // schedule words before the per-tile estimates
+// Header words [kSchedZeroWords, kSchedHeader) outlive a forward: the automatic kernel choice (see
+// plan_forward) keeps there the packet counts of the last scheduled forward and the choice the scan
+// kernel made from them; only the words before them are cleared at the start of a schedule.
+constexpr int kSchedZeroWords = 48;
+constexpr int kStatPackets = 48;   // packets traced by the last scheduled forward
+constexpr int kStatRetraced = 49;  // of them, packets that need more than one traversal with 16 slots
+constexpr int kStatChoice = 50;    // kernel of the automatic choice: kChoiceNarrow or kChoiceWide
+constexpr uint32_t kChoiceNarrow = 1u, kChoiceWide = 2u;
+// the wide kernel (32 hit slots, four blocks per SM) is chosen when more than kWideSixteenths / 16
+// of the last forward's packets need more than one traversal with 16 slots (counted the same way by
+// both kernels, so the choice does not depend on which one ran), the narrow one (16 slots, six blocks
+// per SM) otherwise
+constexpr uint32_t kWideSixteenths = 2u;
 // Per pixel tile, the BVH frontier its frustum reaches (kFrontierWords words: count, then up to
 // kFrontierMax node or leaf entries); a count of kFrontierNone means "start at the root".  A frontier
 // goes onto the traversal stack, so it leaves room there for the traversal's own pushes (up to 64
@@ -61,6 +74,7 @@ struct FwdArgs {
     const uint8_t *render_ellipsoids;
     const float *ellipsoid_min_opacity;
     int display;  // forward_pass_display: colour only, whatever grads_enabled holds
+    int auto_role;  // 0, or kChoiceNarrow / kChoiceWide: the launch of the automatic choice this is
     uint32_t *schedule;  // work order of the pixel tiles (null: tiles in launch order)
     int tiles_x, ntiles;
     uint32_t *frontier;  // per-tile BVH frontiers (null: packets start at the root)
@@ -159,6 +173,7 @@ struct RayResult {
     LaneState st;
     int nacc;
     uint32_t head;
+    bool retraced;  // the packet traversed, or with 16 hit slots would have traversed, more than once
 };
 
 // Intersection program + all-hit sums + selection for one (ray, Gaussian) pair whose snapshot rows,
@@ -560,6 +575,9 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
 
     bool first = true;
     int traversals = 0;
+    // the packet needs a second traversal with a 16-slot buffer: some lane of a 32-slot kernel goes
+    // on past the 16 nearest keys of its first traversal (the same 16 the narrow kernel holds)
+    bool deep = false;
     const int n = sc.n;
     while (__any_sync(kFull, !done)) {
         const bool want = !done;
@@ -658,6 +676,9 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
             const int t = threadIdx.x;
             const unsigned long long last_key = st.kcount > 0 ? kbuf[st.kcount - 1][t] : 0ull;
             for (int i = 0; i < st.kcount; i++) {
+                if constexpr (KB > 16) {
+                    if (i == 16 && first) deep = true;
+                }
                 const unsigned long long key = kbuf[i][t];
                 const float d = h2f_bits((uint16_t)(key >> 48));
                 if (!(d > tmin_sel)) continue;
@@ -764,6 +785,7 @@ __device__ __forceinline__ void trace_ray(const TraceScene &sc, const TraceKnobs
     res.depth = depth;
     res.nacc = nacc;
     res.head = head;
+    res.retraced = __any_sync(kFull, traversals > 0 || deep);
 }
 
 // Truncated-tail estimate and background (cuda/forward_pass.cu:131-142).
@@ -820,7 +842,7 @@ struct FwdShared {
 // Packet (wx, wy) of pixel tile (bx, by) (a tile is 2x2 packets of tile_w x tile_h pixels), traced
 // by the calling warp; front_base + front_off: the tile's BVH frontier (count, entries), or a null base.
 template <int KB>
-__device__ __forceinline__ void forward_packet(const FwdArgs &a, int bx, int by, int wx, int wy,
+__device__ __forceinline__ bool forward_packet(const FwdArgs &a, int bx, int by, int wx, int wy,
                                                const uint32_t *front_base, uint32_t front_off, FwdShared<KB> &sh) {
     unsigned long long(*kbuf)[kFwdThreads] = sh.kbuf;
     Frustum *sfr = sh.sfr;
@@ -876,10 +898,10 @@ __device__ __forceinline__ void forward_packet(const FwdArgs &a, int bx, int by,
     trace_ray<KB>(sc, k, ro, rd, alive, grads, hs, a.status, kbuf, r, frustum ? &sfr[warp] : nullptr, sh.sstk[warp],
                   sh.scand[warp], &sh.scc[warp], frustum ? front_base : nullptr, front_off);
 
-    if (!inside) return;
+    if (!inside) return r.retraced;
     if (!alive) {
         a.head[pixel] = GRAY_NULL;  // inactive pixel: empty list, nothing else written
-        return;
+        return r.retraced;
     }
     float r0, r1, r2;
     finish_ray(r, a.bg, *a.eps_fwd, k.render_depth, r0, r1, r2);
@@ -912,12 +934,14 @@ __device__ __forceinline__ void forward_packet(const FwdArgs &a, int bx, int by,
         }
         a.head[pixel] = GRAY_NULL;
     }
+    return r.retraced;
 }
 
 // One block's pixel tile (bx, by): its four packets, one per warp; the tile's frontier is copied
-// into shared memory once by the block.
+// into shared memory once by the block.  Returns whether the calling warp's packet needs more than
+// one traversal with 16 hit slots (RayResult::retraced).
 template <int KB>
-__device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, FwdShared<KB> &sh) {
+__device__ __forceinline__ bool forward_tile(const FwdArgs &a, int bx, int by, FwdShared<KB> &sh) {
     const int warp = threadIdx.x >> 5;
     {   // every thread of the block gets here together
         const uint32_t *src = a.frontier ? a.frontier + (size_t)(by * a.tiles_x + bx) * kFrontierWords : nullptr;
@@ -928,7 +952,7 @@ __device__ __forceinline__ void forward_tile(const FwdArgs &a, int bx, int by, F
         if (threadIdx.x == 0) sh.front[0] = use ? cnt : kFrontierNone;
         __syncthreads();
     }
-    forward_packet<KB>(a, bx, by, warp % kBlockWarpsX, warp / kBlockWarpsX, sh.front, 0u, sh);
+    return forward_packet<KB>(a, bx, by, warp % kBlockWarpsX, warp / kBlockWarpsX, sh.front, 0u, sh);
 }
 
 // Grid launch: block (x, y) renders tile (x, y).
@@ -941,19 +965,37 @@ __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_kernel(const 
 
 // Persistent launch: the blocks take tiles from the schedule's order, densest first, until none is
 // left (a separate kernel, so the grid launch keeps its register allocation).
+// The packets it traced, and those that traverse more than once with a 16-slot buffer (whatever KB
+// is), are added to the schedule's statistics words (the automatic kernel choice of the next forward
+// reads them).
 template <int KB, int MINB>
 __global__ void __launch_bounds__(kFwdThreads, MINB) trace_forward_sched_kernel(const FwdArgs a) {
     __shared__ FwdShared<KB> sh;
-    __shared__ uint32_t s_next;
+    __shared__ uint32_t s_next, s_packets, s_retraced;
     if (*a.render_ellipsoids) return;
+    // automatic choice: both kernels are launched, the one the scan kernel did not choose leaves
+    if (a.auto_role != 0 && a.schedule[kStatChoice] != (uint32_t)a.auto_role) return;
+    if (threadIdx.x == 0) {
+        s_packets = 0u;
+        s_retraced = 0u;
+    }
     for (;;) {
-        __syncthreads();  // every thread is done with the previous tile (s_next, the frontier)
+        __syncthreads();  // every thread is done with the previous tile (s_next, the frontier, counts)
         if (threadIdx.x == 0) s_next = atomicAdd(a.schedule, 1u);
         __syncthreads();
         const uint32_t t = s_next;
         if (t >= (uint32_t)a.ntiles) break;
         const uint32_t tile = a.schedule[kSchedHeader + a.ntiles + t];
-        forward_tile<KB>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x), sh);
+        const bool again =
+            forward_tile<KB>(a, (int)(tile % (uint32_t)a.tiles_x), (int)(tile / (uint32_t)a.tiles_x), sh);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&s_packets, 1u);
+            if (again) atomicAdd(&s_retraced, 1u);
+        }
+    }
+    if (threadIdx.x == 0 && s_packets > 0u) {
+        atomicAdd(&a.schedule[kStatPackets], s_packets);
+        atomicAdd(&a.schedule[kStatRetraced], s_retraced);
     }
 }
 
@@ -1338,6 +1380,8 @@ __global__ void __launch_bounds__(32) tile_cost_kernel(const FwdArgs a, int bw, 
     }
 }
 
+// Bucket offsets of the densest-first order; and the automatic kernel choice for this forward from
+// the last scheduled forward's packet counts (the narrow kernel when there are none yet).
 __global__ void sched_scan_kernel(uint32_t *sched) {
     if (threadIdx.x != 0) return;
     uint32_t acc = 0;
@@ -1346,6 +1390,15 @@ __global__ void sched_scan_kernel(uint32_t *sched) {
         sched[1 + k] = acc;
         acc += c;
     }
+    const uint32_t packets = sched[kStatPackets], retraced = sched[kStatRetraced];
+    uint32_t choice = sched[kStatChoice];
+    if (choice != kChoiceNarrow && choice != kChoiceWide) choice = kChoiceNarrow;
+    if (packets > 0u && retraced <= packets)
+        choice = (unsigned long long)retraced * 16ull > (unsigned long long)packets * kWideSixteenths ? kChoiceWide
+                                                                                                     : kChoiceNarrow;
+    sched[kStatChoice] = choice;
+    sched[kStatPackets] = 0u;
+    sched[kStatRetraced] = 0u;
 }
 
 __global__ void sched_scatter_kernel(uint32_t *sched, int ntiles) {
@@ -1656,6 +1709,7 @@ __global__ void __launch_bounds__(kFwdThreads, MINB)
 static FwdArgs forward_args(const gray_params &p, bool display) {
     FwdArgs a;
     a.display = display ? 1 : 0;
+    a.auto_role = 0;
     a.alloc_w = p.image_width;
     a.render_w = p.render_width;
     a.render_h = p.render_height;
@@ -1727,6 +1781,7 @@ cudaError_t launch_ellipsoids(const gray_params &p, bool display, cudaStream_t s
 struct FwdPlan {
     FwdArgs a;
     const void *kern;
+    const void *kern_wide;  // automatic choice: the wide kernel, launched after `kern` (else null)
     dim3 grid;
     int bw, bh;
     bool sched;
@@ -1741,9 +1796,15 @@ static FwdPlan plan_forward(const gray_params &p, bool display) {
     // variant: bits 0-1 select (buffer size, register cap), bit 2 the packet shape, bits 3-4 the
     // tile frontier's cut (64 leaves, 32, 128, no frontier), bit 5 packets claimed per warp
     // (trace_forward_claim_kernel) instead of tiles per block
+    // variant 0 (the default) chooses between the narrow and the wide kernel of kDefaultTraceVariant's
+    // packet shape and cut from the last scheduled forward's re-traversals: the 16-slot hit buffer with
+    // six blocks per SM is faster where few rays composite more than 16 hits, the 32-slot one with
+    // four blocks where many do (a re-traversal repeats the packet's whole traversal)
+    const bool automatic = p.trace_variant <= 0;
     const int v = p.trace_variant > 0 ? p.trace_variant : kDefaultTraceVariant;
     const int fcut = (v >> 3) & 3;
     const bool claim = (v & 32) != 0;
+    q.kern_wide = nullptr;
     a.tile_w = (v & 4) ? 4 : 8;
     a.tile_h = 32 / a.tile_w;
     q.bw = a.tile_w * kBlockWarpsX;
@@ -1767,6 +1828,10 @@ static FwdPlan plan_forward(const gray_params &p, bool display) {
 #undef GRAY_FWD_KERNEL
     if (q.sched) {
         a.schedule = p.hitlist.schedule;
+        if (automatic) {
+            q.kern = reinterpret_cast<const void *>(&trace_forward_sched_kernel<16, 6>);
+            q.kern_wide = reinterpret_cast<const void *>(&trace_forward_sched_kernel<32, 4>);
+        }
         a.frontier_cut = fcut == 0 ? kFrontierCutDefault : fcut == 1 ? 32u : fcut == 2 ? 128u : 0u;
         if (a.frontier_cut > 0 && (size_t)a.ntiles <= (words - kSchedHeader) / (2 + kFrontierWords))
             a.frontier = a.schedule + kSchedHeader + 2 * (size_t)a.ntiles;
@@ -1792,7 +1857,7 @@ cudaError_t launch_trace_schedule(const gray_params &p, bool display, cudaStream
     if (!q.sched) return cudaSuccess;
     // densest tiles first: per-tile estimate and frontier, bucket by log2 of the estimate, order
     cudaError_t e;
-    if ((e = cudaMemsetAsync(q.a.schedule, 0, sizeof(uint32_t) * kSchedHeader, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(q.a.schedule, 0, sizeof(uint32_t) * kSchedZeroWords, s)) != cudaSuccess) return e;
     if (q.nsuper > 0) super_cost_kernel<<<q.nsuper, 32, 0, s>>>(q.a, q.bw, q.bh, q.nsuper);
     tile_cost_kernel<<<q.a.ntiles, 32, 0, s>>>(q.a, q.bw, q.bh);
     sched_scan_kernel<<<1, 32, 0, s>>>(q.a.schedule);
@@ -1803,20 +1868,30 @@ cudaError_t launch_trace_schedule(const gray_params &p, bool display, cudaStream
 cudaError_t launch_trace_forward(const gray_params &p, bool display, bool schedule_ready, cudaStream_t s) {
     FwdPlan q = plan_forward(p, display);
     cudaError_t e;
-    dim3 grid = q.grid;
-    if (q.sched) {
-        if (!schedule_ready && (e = launch_trace_schedule(p, display, s)) != cudaSuccess) return e;
-        // a persistent grid that takes the tiles in the schedule's order
-        int dev = 0, sms = 0, per_sm = 0;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, q.kern, kFwdThreads, 0)) != cudaSuccess)
+    if (!q.sched) {
+        void *args[] = {&q.a};
+        if ((e = cudaLaunchKernel(q.kern, q.grid, dim3(kFwdThreads), args, 0, s)) != cudaSuccess) return e;
+        return cudaGetLastError();
+    }
+    if (!schedule_ready && (e = launch_trace_schedule(p, display, s)) != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    // persistent grids that take the tiles in the schedule's order; with the automatic choice both
+    // kernels are launched and the one not chosen returns at once
+    const void *kerns[2] = {q.kern, q.kern_wide};
+    const int roles[2] = {q.kern_wide ? (int)kChoiceNarrow : 0, (int)kChoiceWide};
+    for (int i = 0; i < 2 && kerns[i]; i++) {
+        int per_sm = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kerns[i], kFwdThreads, 0)) != cudaSuccess)
             return e;
         const unsigned int want = (unsigned int)(sms * (per_sm > 0 ? per_sm : 1));
-        grid = dim3(want < (unsigned int)q.a.ntiles ? want : (unsigned int)q.a.ntiles, 1, 1);
+        const dim3 grid(want < (unsigned int)q.a.ntiles ? want : (unsigned int)q.a.ntiles, 1, 1);
+        FwdArgs a = q.a;
+        a.auto_role = roles[i];
+        void *args[] = {&a};
+        if ((e = cudaLaunchKernel(kerns[i], grid, dim3(kFwdThreads), args, 0, s)) != cudaSuccess) return e;
     }
-    void *args[] = {&q.a};
-    if ((e = cudaLaunchKernel(q.kern, grid, dim3(kFwdThreads), args, 0, s)) != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

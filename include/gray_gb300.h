@@ -170,11 +170,14 @@ typedef struct gray_params {
     gray_hitlist hitlist;
     gray_scene scene;
     int32_t *status; /* device int32, GRAY_STATUS_* bits */
-    /* forward-trace kernel variant (0 = library default): bits 0-1 = physical hit buffer of
-     * 32 or 16 keys and register cap, bit 2 = 8x4 or 4x8 pixel packets, bits 3-4 = where a pixel
-     * tile's traversals start (BVH nodes of at most 64, 32 or 128 leaves that the tile's frustum
-     * reaches, or the root), bit 5 = how the scheduled launch hands out work (one pixel tile per
-     * block, or one packet per warp).
+    /* forward-trace kernel variant: bits 0-1 = physical hit buffer of 32 or 16 keys and register
+     * cap, bit 2 = 8x4 or 4x8 pixel packets, bits 3-4 = where a pixel tile's traversals start (BVH
+     * nodes of at most 64, 32 or 128 leaves that the tile's frustum reaches, or the root), bit 5 =
+     * how the scheduled launch hands out work (one pixel tile per block, or one packet per warp).
+     * 0 (default): 4x8 packets from 64-leaf frontiers, with the 16-key buffer (six blocks per SM)
+     * or the 32-key one (four blocks per SM) chosen on the device from the previous scheduled
+     * forward of the same schedule buffer (the 32-key one when more than 1/8 of its packets
+     * traversed more than once); both kernels are launched and the one not chosen returns at once.
      * Results are identical for every variant; only speed differs. */
     int32_t trace_variant;
 } gray_params;

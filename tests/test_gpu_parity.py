@@ -620,7 +620,7 @@ def test_clustered_scene_with_bvh(oracle):
     _compare_forward(rt, fwd)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 15, 23, 31, 8 + 3, 32 + 7, 32 + 1, 32 + 4, 32 + 31])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7, 15, 23, 31, 8 + 3, 32 + 7, 32 + 1, 32 + 4, 32 + 31])
 def test_trace_variants_are_bit_identical(oracle, variant):
     """Every forward-kernel variant (hit buffer size, register cap, packet shape, tile frontier cut
     of 64, 32 or 128 leaves or none, one tile per block or one packet per warp) gives the same bits
@@ -639,6 +639,42 @@ def test_trace_variants_are_bit_identical(oracle, variant):
                                bvh=oracle.Bvh(aabb, vis))
     assert fwd["nacc"].max() > 20  # more than one 16-key buffer on some rays
     _compare_forward(rt, fwd)
+
+
+def test_automatic_kernel_choice_follows_the_last_forwards_re_traversals(oracle):
+    """Default variant: the scheduled kernels count the packets that need more than one traversal
+    with 16 hit slots (the same count from the 16-slot and the 32-slot kernel: packets with a ray
+    that composites more than 16 hits), and the next forward runs the 32-slot kernel when more than
+    1/8 of the packets do; the image equals the oracle's whichever kernel ran."""
+    sc = synthetic.clustered_scene(40_000, seed=8)
+    chan = np.random.default_rng(2).uniform(0, 1, (sc.n, 3)).astype(np.float32)
+    W, H = 72, 56
+    scale = sc.scale + np.float32(1.5)
+    geom, l2w, aabb, vis, live = _oracle_scene(oracle, sc.mean, sc.rotation, scale, sc.opacity)
+    cam = synthetic.orbit_camera(1.1, W, H, radius=4.0)
+    words = {}
+    for t_thr in (0.001, 0.6):  # rays composite many hits / stop after a few
+        rt = G.make_tracer(W, H, sc.mean, sc.rotation, scale, sc.opacity, channels=chan, t_threshold=t_thr)
+        counts = {}
+        for v in (7, 5, 0, 0):
+            rt.set_trace_variant(v)
+            rt.get_stats().reset()  # per-pixel hit counts accumulate over forwards
+            ro, rd = _camera_rays_gpu(rt, cam)
+            counts[v] = rt.schedule[48:51].cpu().tolist()
+        fwd = oracle.trace_forward(ro, rd, geom, live, chan, vis, oracle.TraceConfig(t_threshold=t_thr),
+                                   bvh=oracle.Bvh(aabb, vis))
+        _compare_forward(rt, fwd)
+        packets = 9 * 4 * 4  # 8x16-pixel tiles of four 4x8 packets
+        assert counts[7][0] == counts[5][0] == counts[0][0] == packets
+        assert counts[7][1] == counts[5][1] == counts[0][1]  # the same count from either kernel
+        nacc = np.zeros((64, W), np.int64)
+        nacc[:H] = fwd["nacc"].reshape(H, W)
+        deep_rays = nacc.reshape(8, 8, W // 4, 4).transpose(0, 2, 1, 3).reshape(-1, 32).max(axis=1) > 16
+        assert abs(counts[0][1] - int(deep_rays.sum())) <= 2, (counts[0][1], int(deep_rays.sum()))
+        words[t_thr] = counts[0]
+    deep, shallow = words[0.001], words[0.6]
+    assert deep[1] * 8 > deep[0] and deep[2] == 2      # many packets need a second traversal: 32 slots
+    assert shallow[1] * 8 <= shallow[0] and shallow[2] == 1
 
 
 def test_copy_wait_runs_out_reports_and_leaves_the_context_usable(oracle):
