@@ -56,6 +56,9 @@ def parse_args(argv):
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--no-served", action="store_true", help="skip the served measurement only")
     ap.add_argument("--trace-variant", type=int, default=0, help="forward-kernel variant (0 = library default)")
+    ap.add_argument("--view", type=int, default=-1,
+                    help="clustered scene: train on the pose of view K of the batched form's 16 jittered orbit "
+                         "views (at --width x --height) instead of the default orbit camera")
     ap.add_argument("--record-traffic", nargs="+", metavar="ARG",
                     help="CSV KEY KERNEL [UNITS_SCALE]: store the per-launch DRAM bytes of KERNEL in an ncu CSV "
                          "capture under KEY in profiles/ncu_traffic.json, with the digest of the current kernel "
@@ -79,7 +82,8 @@ def apply_scene(a):
 def workload_config(a, rank=0):
     kind = {"clustered": "clustered", "small": "uniform [-1,1]^3", "gradcheck": "uniform [-2,2]^3"}[a.scene]
     count = f"{a.n_gaussians / 1e6:g}M" if a.n_gaussians >= 100_000 else f"{a.n_gaussians}"
-    return {"workload": f"train step, {count} {kind} Gaussians, {a.width}x{a.height}",
+    view = f", jittered view {a.view}" if a.view >= 0 and a.scene == "clustered" else ""
+    return {"workload": f"train step, {count} {kind} Gaussians, {a.width}x{a.height}{view}",
             "n_gaussians": a.n_gaussians, "width": a.width, "height": a.height, "rays_per_step": a.width * a.height,
             "sh_degree": 3, "t_threshold": 0.03, "alpha_threshold": 0.01, "exp_power": 2.0,
             "l2": "inputs larger than L2 (no flush)" if a.scene == "clustered" and a.n_gaussians >= 1_000_000
@@ -103,6 +107,8 @@ def make_camera(a, rank):
         return synthetic.camera_small(a.width, a.height)
     if a.scene == "gradcheck":
         return synthetic.camera_small(a.width, a.height, focal=float(a.width))
+    if a.view >= 0:
+        return synthetic.uneven_view(a.view, a.width, a.height)
     return synthetic.orbit_camera(0.3 + 0.7 * rank, a.width, a.height)
 
 

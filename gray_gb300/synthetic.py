@@ -110,3 +110,12 @@ def uneven_cameras(count: int = 16, seed: int = 0, resolutions=None) -> list[Cam
         jit = tuple(rng.uniform(-math.radians(15), math.radians(15), 2))
         cams.append(orbit_camera(2 * math.pi * i / count, w, h, jitter_rad=jit, uid=i))
     return cams
+
+
+def uneven_view(k: int, width: int, height: int, count: int = 16, seed: int = 0) -> CameraInfo:
+    """The pose of uneven_cameras(count, seed)[k] at width x height."""
+    c = uneven_cameras(count, seed)[k % count]
+    fov_y = 2.0 * math.atan(0.5 * height / (0.75 * width))
+    return CameraInfo(uid=c.uid, R=c.R, T=c.T, origin=c.origin, fov_y=fov_y,
+                      fov_x=2.0 * math.atan(math.tan(fov_y / 2.0) * width / height), image_width=width,
+                      image_height=height)
